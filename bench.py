@@ -1,0 +1,349 @@
+"""Benchmark of the drawable-processing pass on GB300.
+
+Default workload: the plain pass on the large CAD scene (C2: 16,777,216
+drawables in 256 StateSets, hierarchy 4,096 -> 65,536 -> 1,048,576 ->
+drawables, 3 LODs, seed 1).  One step = one full pass: propagation of every
+hierarchy level, then the fused leaf kernel (world matrices, bounding
+spheres, frustum cull, LOD, per-StateSet compaction).
+
+  value  Gdrawables/s with the scene resident in HBM (inputs 1.6 GB > L2, so
+         no L2 flush between steps is needed)
+  e2e    same metric through the C ABI with host buffers: every step uploads
+         all per-drawable inputs from pinned host memory, runs the pass and
+         reads the per-StateSet counts and the visible commands back
+  roofline  the fused leaf kernel's algorithmic bytes per launch over its
+         average launch time (CUDA events on the launching stream)
+
+`--impl reference` times the CPU restatement of the pass (the oracle,
+OpenMP over all host cores) on the same workload: the reference itself has
+no CPU implementation of the pass, and its GPU path (Vulkan shaders) cannot
+run without a graphics stack.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gdrawables/s culled+compacted"
+UNIT = "Gdrawables/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=16_777_216, help="drawables of the C2 scene")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (default: min(steps, 50))")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM traffic of the leaf kernel on the full C2 scene from
+    the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "leaf_cull_c2.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.lines = index, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def leaf_algorithmic_bytes(sc, visible: int) -> int:
+    """Compulsory DRAM bytes of one fused leaf launch: per drawable the local
+    matrix (64), parent index (4), local sphere (16), geometry index (4) and
+    world matrix written (64); per visible drawable its 20-byte command; the
+    marginal bitmask (N/8); every parent world matrix read once."""
+    n = sc.n
+    parents = sc.level_sizes[-1] if sc.level_sizes else 0
+    return n * (64 + 4 + 16 + 4 + 64) + 20 * visible + (n + 7) // 8 + 64 * parents
+
+
+def step_algorithmic_bytes(sc, visible: int) -> int:
+    """The whole step: the leaf launch plus every internal level l >= 1
+    (local read 64, parent index 4, world write 64, parents read once)."""
+    b = leaf_algorithmic_bytes(sc, visible)
+    sizes = sc.level_sizes
+    for l in range(1, len(sizes)):
+        b += sizes[l] * (64 + 4 + 64) + sizes[l - 1] * 64
+    return b
+
+
+def run_reference(args, sc, world, rank):
+    """CPU restatement of the pass (the oracle) on all host cores."""
+    from oracle import bind
+    threads = bind.max_threads()
+    view = sc.views[0]
+    for _ in range(max(0, min(args.warmup, 1))):
+        bind.cull(sc, view, threads=threads)
+    steps = max(1, min(args.steps, 3))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        bind.cull(sc, view, threads=threads)
+        times.append(time.perf_counter() - t0)
+    ms = float(np.median(times)) * 1e3
+    value = sc.n / (ms / 1e3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"C2 plain pass, {sc.n} drawables, 256 StateSets, 3 LODs, seed 1",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full C2 scene ({sc.n} drawables), median of {steps} passes "
+                                   "(bench steps capped at 3 to bound the run)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference" and rank != 0:
+        return
+    from cadr_gb300 import scenes
+    t0 = time.time()
+    sc = scenes.config2(n=args.n)
+    gen_s = time.time() - t0
+    if args.impl == "reference":
+        import oracle
+        oracle.build(with_ref=False)
+        run_reference(args, sc, world, rank)
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from cadr_gb300 import build, lib
+    build.build()
+    ctx = lib.Context(local)
+    ds = lib.DeviceScene(ctx, sc)
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    view = sc.views[0]
+    L = ctx.lib
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- device-resident timed region ------------------------------------
+    for _ in range(args.warmup):
+        ds.cull(view, out)
+    ctx.sync()
+    ctx.check_device_error()
+    counts = ctx.download(out.counts, np.uint32, (sc.num_state_sets,))
+    visible = int(counts.sum())
+
+    import torch
+    torch.cuda.set_device(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ctx.collect_frame_info(True)
+    barrier()
+    ctx.sync()
+    launches0 = ctx.launch_count
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ds.cull(view, out)
+    ev1.record(stream)
+    ctx.sync()
+    barrier()
+    launches = ctx.launch_count - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    frames = ctx.frame_infos()
+    ctx.collect_frame_info(False)
+    ctx.check_device_error()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    leaf_ms = float(np.mean([f[1] for f in frames])) if frames else None
+    prop_ms = float(np.mean([f[0] for f in frames])) if frames else None
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    e2e_steps = args.e2e_steps or min(args.steps, 50)
+    pin = {}
+    for name, a in [("local", sc.local), ("parent", sc.parent), ("sphere", sc.sphere), ("geometry", sc.geometry)]:
+        b = lib.PinnedBuffer(a.nbytes)
+        b.view(a.dtype, a.shape)[...] = a
+        pin[name] = b
+    lvl_pin = []
+    for loc, par in zip(sc.level_local, sc.level_parent):
+        bl = lib.PinnedBuffer(loc.nbytes)
+        bl.view(loc.dtype, loc.shape)[...] = loc
+        bp = None
+        if par is not None:
+            bp = lib.PinnedBuffer(par.nbytes)
+            bp.view(par.dtype, par.shape)[...] = par
+        lvl_pin.append((bl, bp, loc.shape[0]))
+    h_counts = lib.PinnedBuffer(sc.num_state_sets * 4)
+    h_cmds = lib.PinnedBuffer(sc.n * 20)
+    offs = sc.state_set_offsets.astype(np.int64)
+    h2d = sum(b.nbytes for b in pin.values()) + sum(bl.nbytes + (bp.nbytes if bp else 0) for bl, bp, _ in lvl_pin)
+
+    def e2e_step():
+        for l, (bl, bp, n_l) in enumerate(lvl_pin):
+            lib.check(L.cadr_scene_upload_level(ds.handle, l, bl.ptr, bp.ptr if bp else None, 0, n_l))
+        lib.check(L.cadr_scene_upload_drawables(ds.handle, pin["local"].ptr, pin["parent"].ptr,
+                                                pin["sphere"].ptr, pin["geometry"].ptr, 0, sc.n))
+        ds.cull(view, out)
+        lib.check(L.cadr_download(ctx.handle, h_counts.ptr, out.counts.ptr, sc.num_state_sets * 4, None))
+        lib.check(L.cadr_stream_synchronize(ctx.stream))
+        cnt = h_counts.view(np.uint32, (sc.num_state_sets,))
+        d2h = sc.num_state_sets * 4
+        for s in range(sc.num_state_sets):
+            c = int(cnt[s])
+            if c:
+                lib.check(L.cadr_download(ctx.handle, h_cmds.ptr + int(offs[s]) * 20,
+                                          out.cmds.ptr + int(offs[s]) * 20, c * 20, None))
+                d2h += c * 20
+        lib.check(L.cadr_stream_synchronize(ctx.stream))
+        return d2h
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t1 = time.perf_counter()
+    d2h_total = 0
+    for _ in range(e2e_steps):
+        d2h_total += e2e_step()
+    e2e_s = (time.perf_counter() - t1) / e2e_steps
+    barrier()
+    clk = clocks.stop()
+    e2e_value = world * sc.n / e2e_s / 1e9
+
+    value = world * sc.n / (ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    leaf_bytes = leaf_algorithmic_bytes(sc, visible)
+    achieved = leaf_bytes / (leaf_ms / 1e3) / 1e9 if leaf_ms else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"C2 plain pass, {sc.n} drawables, 256 StateSets (Zipf 1.1), levels "
+                               f"{sc.level_sizes}, 3 LODs, seed 1",
+                   "visible_fraction": visible / sc.n, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": committed_traffic(),
+                     "kernel": "leaf_kernel<true> (fused propagate+sphere+cull+LOD+compact)",
+                     "algorithmic_bytes_per_launch": leaf_bytes, "launch_ms": leaf_ms,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "step": {"propagate_ms": prop_ms, "leaf_ms": leaf_ms,
+                 "step_algorithmic_bytes": step_algorithmic_bytes(sc, visible),
+                 "step_gbs": step_algorithmic_bytes(sc, visible) / (ms / 1e3) / 1e9},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h_total // max(1, e2e_steps), "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "scene_generation_s": gen_s,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import bind
+        import oracle
+        oracle.build(with_ref=False)
+        threads = bind.max_threads()
+        ts = []
+        for _ in range(3):
+            t2 = time.perf_counter()
+            bind.cull(sc, view, threads=threads)
+            ts.append(time.perf_counter() - t2)
+        cms = float(np.median(ts))
+        line["cpu_baseline"] = {"value": sc.n / cms / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"full C2 scene ({sc.n} drawables), median of 3 passes"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,370 @@
+// batched.cu - the batched form: many (scene, view) pairs culled by one
+// persistent launch over (view, tile) work items.
+//
+// Scenes are propagated once (cadr_scene_propagate with world spheres); each
+// view then reads only the 16-byte world sphere and the 4-byte geometry
+// index of every drawable.  Work items are numbered view-major and handed
+// out by an atomic counter, so the items a tile looks back on were taken
+// earlier by resident CTAs.  The arithmetic per (view, drawable) is the
+// plain pass's (same classify, same compaction), so outputs are identical.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "capi_internal.h"
+#include "compact.cuh"
+
+namespace cadr {
+
+struct BatchedState {
+    ViewJob* d_jobs = nullptr;
+    ViewJob* h_jobs = nullptr;  // pinned; read by the graph's copy node
+    uint32_t cap = 0;
+    cudaEvent_t jobs_free = nullptr;
+    bool jobs_pending = false;
+    Scratch scratch;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t key_views = 0, key_items = 0, key_grid = 0;
+    cadr_tuning key_tuning = {};
+    cudaStream_t key_stream = nullptr;
+};
+
+namespace {
+
+template <int THREADS, int IPT>
+__global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
+                                                         uint32_t total_items, const Scratch s, uint32_t* error,
+                                                         uint64_t limit_ns)
+{
+    using T = Tile<THREADS, IPT>;
+    __shared__ typename T::Smem sm;
+    __shared__ __align__(16) ViewJob job;
+    __shared__ uint32_t s_job;
+
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) sm.info[1] = load_relaxed_u32(&s.ctl->epoch);
+    uint32_t cur_job = 0xffffffffu;
+    for (;;) {
+        if (t == 0) {
+            const uint32_t item = atomicAdd(&s.ctl->tile_counter, 1u);
+            sm.info[0] = item;
+            uint32_t lo = 0, hi = num_jobs;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(&jobs[mid].first_item) <= item)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            s_job = lo ? lo - 1 : 0;
+        }
+        __syncthreads();
+        const uint32_t item = sm.info[0];
+        if (item >= total_items) break;
+        if (s_job != cur_job) {
+            cur_job = s_job;
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + cur_job);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&job);
+            for (int k = t; k < (int)(sizeof(ViewJob) / 4); k += THREADS) dst[k] = __ldg(src + k);
+            __syncthreads();
+        }
+        const uint32_t b = (item - job.first_item) * (uint32_t)T::SIZE;
+        uint32_t vis_bits = 0, lod_bits = 0;
+        uint32_t geo[IPT];
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const uint32_t i = b + (uint32_t)(j * THREADS + t);
+            bool visible = false, marginal = false;
+            uint32_t lod = 0;
+            geo[j] = 0;
+            if (i < job.n) {
+                const float4 ws = ld_nc_f4(job.world_sphere + i);
+                geo[j] = ld_nc_u32(job.geometry + i);
+                classify(job.view, ws, job.num_lods, visible, marginal, lod);
+            }
+            const uint32_t vb = __ballot_sync(~0u, visible);
+            const uint32_t mb = __ballot_sync(~0u, marginal);
+            const uint32_t word0 = b + (uint32_t)(j * THREADS + warp * kWarp);
+            if (lane == 0) {
+                sm.ballot[j][warp] = vb;
+                if (job.marginal && word0 < job.n) job.marginal[word0 >> 5] = mb;
+            }
+            vis_bits |= (visible ? 1u : 0u) << j;
+            lod_bits |= lod << (2 * j);
+        }
+        __syncthreads();
+        T::scan(sm, job.offsets, job.num_state_sets, b, job.n);
+        T::lookback(sm, s.tile_state, item, job.first_item, job.offsets, b, limit_ns, 0u, error);
+        T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, job.offsets, job.num_state_sets,
+                 job.lods, job.num_geometries, job.num_lods, job.cmds, job.counts, error);
+        __syncthreads();
+    }
+    if (t == 0) finish_pass(s.ctl);
+}
+
+using KernelFn = void (*)(const ViewJob*, uint32_t, uint32_t, const Scratch, uint32_t*, uint64_t);
+
+template <int TH>
+KernelFn pick_ipt(uint32_t ipt)
+{
+    switch (ipt) {
+    case 4: return batched_kernel<TH, 4>;
+    case 8: return batched_kernel<TH, 8>;
+    case 16: return batched_kernel<TH, 16>;
+    }
+    return nullptr;
+}
+
+KernelFn pick_kernel(uint32_t threads, uint32_t ipt)
+{
+    switch (threads) {
+    case 128: return pick_ipt<128>(ipt);
+    case 256: return pick_ipt<256>(ipt);
+    case 512: return pick_ipt<512>(ipt);
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread)
+{
+    return block_threads * items_per_thread;
+}
+
+cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items, Scratch& s,
+                                uint32_t* error, uint64_t spin_limit_ns, uint32_t block_threads,
+                                uint32_t items_per_thread, uint32_t grid, cudaStream_t stream)
+{
+    KernelFn k = pick_kernel(block_threads, items_per_thread);
+    if (!k) return cudaErrorInvalidValue;
+    k<<<grid, block_threads, 0, stream>>>(d_jobs, num_jobs, total_items, s, error, spin_limit_ns);
+    return cudaGetLastError();
+}
+
+void destroy_batched_state(cadr_context* ctx)
+{
+    BatchedState* b = ctx->batched;
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_jobs) cudaFree(b->d_jobs);
+    if (b->h_jobs) cudaFreeHost(b->h_jobs);
+    if (b->jobs_free) cudaEventDestroy(b->jobs_free);
+    scratch_release(b->scratch);
+    delete b;
+    ctx->batched = nullptr;
+}
+
+bool tuning_valid(const cadr_tuning& t)
+{
+    return pick_kernel(t.block_threads, t.items_per_thread) != nullptr && t.ctas_per_sm >= 1 && t.ctas_per_sm <= 16;
+}
+
+// Fills `jobs` for a batch and returns the total number of work items.
+cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, ViewJob* jobs, uint64_t* total)
+{
+    uint64_t items = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        const cadr_batch_view& bv = views[v];
+        cadr_scene* sc = bv.scene;
+        if (!sc) return fail(CADR_ERR_INVALID_ARG, "cull_batched: view %u has no scene", v);
+        if (!sc->committed) return fail(CADR_ERR_INVALID_ARG, "cull_batched: scene of view %u is not committed", v);
+        if (!bv.counts || (!bv.cmds && sc->desc.num_drawables))
+            return fail(CADR_ERR_INVALID_ARG, "cull_batched: view %u has no output buffers", v);
+        ViewJob& j = jobs[v];
+        std::memset(&j, 0, sizeof(j));
+        j.world_sphere = reinterpret_cast<const float4*>(sc->buf.world_sphere);
+        j.geometry = sc->buf.geometry;
+        j.offsets = sc->buf.state_set_offsets;
+        j.lods = reinterpret_cast<const uint4*>(sc->buf.lods);
+        j.cmds = reinterpret_cast<uint32_t*>(bv.cmds);
+        j.counts = bv.counts;
+        j.marginal = bv.marginal;
+        j.n = (uint32_t)sc->desc.num_drawables;
+        j.num_state_sets = sc->desc.num_state_sets;
+        j.num_geometries = sc->desc.num_geometries;
+        j.num_lods = sc->desc.num_lods;
+        // An empty scene still takes one item, which writes its zero counts.
+        j.num_tiles = std::max<uint32_t>(1u, (uint32_t)((sc->desc.num_drawables + tile - 1) / tile));
+        j.first_item = (uint32_t)items;
+        j.view = to_view_const(bv.view);
+        items += j.num_tiles;
+        if (items >= 0xFFFF0000ull) return fail(CADR_ERR_INVALID_ARG, "cull_batched: too many work items");
+    }
+    *total = items;
+    return CADR_OK;
+}
+
+}  // namespace cadr
+
+using namespace cadr;
+
+extern "C" {
+
+CADR_API cadr_status cadr_get_tuning(cadr_context* ctx, cadr_tuning* out)
+{
+    if (!ctx || !out) return fail(CADR_ERR_INVALID_ARG, "get_tuning: null argument");
+    *out = ctx->tuning;
+    return CADR_OK;
+}
+
+CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* t)
+{
+    if (!ctx || !t) return fail(CADR_ERR_INVALID_ARG, "set_tuning: null argument");
+    if (!tuning_valid(*t))
+        return fail(CADR_ERR_INVALID_ARG, "set_tuning: unsupported block %u / items %u / ctas %u", t->block_threads,
+                    t->items_per_thread, t->ctas_per_sm);
+    ctx->tuning = *t;
+    return CADR_OK;
+}
+
+CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view* views, uint32_t num_views,
+                                       const cadr_tuning* tuning, int use_graph, cadr_stream stream)
+{
+    if (!ctx || (!views && num_views)) return fail(CADR_ERR_INVALID_ARG, "cull_batched: null argument");
+    if (num_views == 0) return CADR_OK;
+    const cadr_tuning tu = tuning ? *tuning : ctx->tuning;
+    if (!tuning_valid(tu)) return fail(CADR_ERR_INVALID_ARG, "cull_batched: unsupported tuning");
+    cudaStream_t s = pick_stream(ctx, stream);
+    if (!ctx->batched) ctx->batched = new BatchedState();
+    BatchedState& B = *ctx->batched;
+    cudaError_t e;
+    if (!B.jobs_free) {
+        e = cudaEventCreateWithFlags(&B.jobs_free, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: event");
+    }
+    if (B.jobs_pending) {
+        e = cudaEventSynchronize(B.jobs_free);  // the previous copy has read h_jobs
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: wait for job buffer");
+        B.jobs_pending = false;
+    }
+    if (num_views > B.cap) {
+        if (B.exec) cudaGraphExecDestroy(B.exec);
+        if (B.graph) cudaGraphDestroy(B.graph);
+        B.exec = nullptr;
+        B.graph = nullptr;
+        cudaDeviceSynchronize();
+        if (B.d_jobs) cudaFree(B.d_jobs);
+        if (B.h_jobs) cudaFreeHost(B.h_jobs);
+        B.d_jobs = nullptr;
+        B.h_jobs = nullptr;
+        const uint32_t cap = std::max<uint32_t>(num_views, 64u);
+        e = cudaMalloc(&B.d_jobs, cap * sizeof(ViewJob));
+        if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&B.h_jobs), cap * sizeof(ViewJob), cudaHostAllocDefault);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: job buffers");
+        B.cap = cap;
+    }
+    // Scenes may have pending uploads; order them before the batch.
+    for (uint32_t v = 0; v < num_views; v++) {
+        cadr_status st = scene_prepare(views[v].scene, s);
+        if (st != CADR_OK) return st;
+    }
+    uint64_t total = 0;
+    cadr_status st = build_jobs(views, num_views, batched_tile(tu.block_threads, tu.items_per_thread), B.h_jobs, &total);
+    if (st != CADR_OK) return st;
+    st = scratch_reserve(ctx, B.scratch, total);
+    if (st != CADR_OK) return st;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(total, (uint64_t)tu.ctas_per_sm * ctx->num_sms);
+    const size_t job_bytes = num_views * sizeof(ViewJob);
+
+    if (use_graph) {
+        const bool same = B.exec && B.key_views == num_views && B.key_items == total && B.key_grid == grid &&
+                          B.key_stream == s && std::memcmp(&B.key_tuning, &tu, sizeof(tu)) == 0;
+        if (!same) {
+            if (B.exec) cudaGraphExecDestroy(B.exec);
+            if (B.graph) cudaGraphDestroy(B.graph);
+            B.exec = nullptr;
+            B.graph = nullptr;
+            e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_fail(e, "cull_batched: begin capture");
+            cudaError_t e1 = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
+            cudaError_t e2 = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error,
+                                                 ctx->spin_limit_ns, tu.block_threads, tu.items_per_thread, grid, s);
+            e = cudaStreamEndCapture(s, &B.graph);
+            if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess) {
+                if (B.graph) cudaGraphDestroy(B.graph);
+                B.graph = nullptr;
+                return cuda_fail(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e), "cull_batched: capture");
+            }
+            e = cudaGraphInstantiate(&B.exec, B.graph, 0);
+            if (e != cudaSuccess) return cuda_fail(e, "cull_batched: instantiate");
+            B.key_views = num_views;
+            B.key_items = (uint32_t)total;
+            B.key_grid = grid;
+            B.key_tuning = tu;
+            B.key_stream = s;
+        }
+        e = cudaGraphLaunch(B.exec, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: graph launch");
+    } else {
+        e = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: job copy");
+        e = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error, ctx->spin_limit_ns,
+                                tu.block_threads, tu.items_per_thread, grid, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_batched: launch");
+    }
+    ctx->launches++;
+    B.scratch.launches++;
+    e = cudaEventRecord(B.jobs_free, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cull_batched: record");
+    B.jobs_pending = true;
+    return CADR_OK;
+}
+
+// Autotuner: times every supported (block, items per thread, CTAs per SM)
+// combination on the given batch with CUDA events (median of `reps` runs
+// after one warm-up) and keeps the fastest in the context.
+CADR_API cadr_status cadr_autotune_batched(cadr_context* ctx, const cadr_batch_view* views, uint32_t num_views,
+                                           uint32_t reps, cadr_tuning* best, float* best_ms)
+{
+    if (!ctx || !views || num_views == 0 || !best) return fail(CADR_ERR_INVALID_ARG, "autotune: bad argument");
+    if (reps == 0) reps = 5;
+    const uint32_t threads[] = {128, 256, 512};
+    const uint32_t ipts[] = {4, 8, 16};
+    const uint32_t ctas[] = {2, 4, 8};
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaStream_t s = ctx->stream;
+    float best_t = 1e30f;
+    cadr_tuning best_tu = ctx->tuning;
+    for (uint32_t th : threads)
+        for (uint32_t ipt : ipts)
+            for (uint32_t c : ctas) {
+                if (th * c > 2048) continue;  // more threads per SM than the hardware holds
+                cadr_tuning tu = {th, ipt, c, 0};
+                std::vector<float> ts;
+                for (uint32_t r = 0; r <= reps; r++) {
+                    cudaEventRecord(a, s);
+                    cadr_status st = cadr_cull_batched(ctx, views, num_views, &tu, 0, s);
+                    cudaEventRecord(b, s);
+                    if (st != CADR_OK) {
+                        cudaEventDestroy(a);
+                        cudaEventDestroy(b);
+                        return st;
+                    }
+                    cudaEventSynchronize(b);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (r) ts.push_back(ms);
+                }
+                std::sort(ts.begin(), ts.end());
+                const float med = ts[ts.size() / 2];
+                if (med < best_t) {
+                    best_t = med;
+                    best_tu = tu;
+                }
+            }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx->tuning = best_tu;
+    *best = best_tu;
+    if (best_ms) *best_ms = best_t;
+    return CADR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// capi_internal.h - internal state behind the opaque C ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace cadr {
+constexpr int kRingSlots = 2;
+struct BatchedState;
+}
+
+struct cadr_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;         // default compute stream
+    cudaStream_t upload_stream = nullptr;  // side stream of staged uploads
+    cudaEvent_t upload_done = nullptr;
+    cudaEvent_t pass_done = nullptr;       // orders passes sharing `scratch`
+    bool pass_recorded = false;
+    cudaEvent_t ring_event[cadr::kRingSlots] = {};
+    uint8_t* ring = nullptr;               // pinned staging ring
+    size_t ring_bytes = size_t(64) << 20;
+    int ring_next = 0;
+    std::mutex ring_mu;
+    uint32_t* h_error = nullptr;           // mapped pinned error word
+    uint32_t* d_error = nullptr;
+    uint64_t spin_limit_ns = 1000000000ull;
+    uint32_t fault = 0;
+    std::atomic<uint64_t> launches{0};
+    cadr::Scratch scratch;                 // lookback scratch of plain passes
+    cadr_tuning tuning = {256, 4, 4, 0};
+    cadr::BatchedState* batched = nullptr;
+    // frame timing ring (cadr_frame_info)
+    static constexpr int kFrames = 256;
+    bool collect_frames = false;
+    cudaEvent_t frame_ev[kFrames][3] = {};
+    uint64_t frame_head = 0, frame_tail = 0;
+};
+
+struct cadr_scene {
+    cadr_context* ctx = nullptr;
+    cadr_scene_desc desc = {};
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    cadr_scene_buffers buf = {};
+    std::vector<uint32_t> h_offsets;       // host copy of the StateSet offsets
+    bool committed = false;
+    bool upload_pending = false;
+    cudaEvent_t uploaded = nullptr;
+};
+
+namespace cadr {
+extern thread_local std::string g_last_error;
+cadr_status fail(cadr_status s, const char* fmt, ...);
+cadr_status cuda_fail(cudaError_t e, const char* what);
+cadr_status scratch_reserve(cadr_context* ctx, Scratch& s, uint64_t tiles);
+void scratch_release(Scratch& s);
+cadr_status upload_bytes(cadr_context* ctx, void* dst, const void* src, size_t bytes, cudaStream_t stream);
+cudaStream_t pick_stream(cadr_context* ctx, cadr_stream s);
+void destroy_batched_state(cadr_context* ctx);
+cadr_status scene_prepare(cadr_scene* sc, cudaStream_t stream);
+ViewConst to_view_const(const cadr_view& v);
+cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, ViewJob* jobs, uint64_t* total);
+}  // namespace cadr

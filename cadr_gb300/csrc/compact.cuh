@@ -1,0 +1,228 @@
+// compact.cuh - per-StateSet compaction of one tile of drawables.
+//
+// A tile is THREADS * IPT consecutive drawables; item j of thread t is
+// drawable b + j*THREADS + t, so each warp ballot covers 32 consecutive
+// drawables and the ballots in (j, warp) order are in drawable order.
+// The visible drawables of StateSet s go to cmds[offsets[s] + k] for the
+// k-th visible drawable of that region, in ascending drawable order:
+//   slot(i) = offsets[s] + (number of visible drawables of region s before i)
+// computed as a segmented scan (regions are the segments) whose carry
+// between tiles comes from a decoupled lookback over published tile states.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cadr {
+
+// Segmented decoupled lookback by one warp.  Returns the segmented
+// exclusive prefix at the tile start: the number of flagged items from the
+// start of the region containing the tile's first item up to that item.
+// Lanes inspect 32 predecessors at a time; a predecessor that published its
+// inclusive prefix, or whose aggregate contains a region start, ends the
+// walk.  Items below `first` count as empty terminators.  Every wait is
+// bounded by limit_ns; on expiry timed_out is set and the partial carry
+// returned (the pass then reports CADR_ERR_TIMEOUT).
+__device__ __forceinline__ uint32_t warp_lookback(const uint64_t* __restrict__ states, int64_t item,
+                                                  int64_t first, uint32_t epoch, uint64_t limit_ns,
+                                                  bool& timed_out)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t ep = epoch & kEpochMask;
+    uint32_t carry = 0;
+    int64_t cur = item - 1;
+    uint64_t t0 = 0;
+    for (uint32_t it = 0; it < (1u << 30); it++) {
+        const int64_t idx = cur - lane;
+        uint64_t w = 0;
+        bool valid = true, term = true;
+        if (idx >= first) {
+            w = load_relaxed_u64(states + idx);
+            valid = st_status(w) != 0 && st_epoch(w) == ep;
+            term = valid && (st_status(w) == kStatusPrefix || st_head(w));
+        }
+        const uint32_t tmask = __ballot_sync(~0u, term);
+        const uint32_t vmask = __ballot_sync(~0u, valid);
+        const int ft = tmask ? __ffs(tmask) - 1 : 32;
+        const uint32_t need = (ft >= 31) ? 0xffffffffu : ((2u << ft) - 1u);
+        if ((vmask & need) == need) {
+            uint32_t v = (lane <= ft && idx >= first) ? st_value(w) : 0u;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+            carry += v;
+            if (ft < 32) return carry;
+            cur -= 32;
+            t0 = 0;
+        } else {
+            uint64_t now = global_timer_ns();
+            now = __shfl_sync(~0u, now, 0);
+            if (t0 == 0) {
+                t0 = now;
+            } else if (now - t0 > limit_ns) {
+                timed_out = true;
+                return carry;
+            }
+            __nanosleep(64);
+        }
+    }
+    timed_out = true;
+    return carry;
+}
+
+template <int THREADS, int IPT>
+struct Tile {
+    static constexpr int NW = THREADS / kWarp;
+    static constexpr int NC = IPT * NW;
+    static constexpr int SIZE = THREADS * IPT;
+    static_assert(NW >= 2, "two warps at least");
+
+    struct Smem {
+        uint32_t ballot[IPT][NW];
+        uint32_t prefix[NC];
+        uint32_t info[8];  // 0 item, 1 epoch, 2 carry, 3 total, 4 first region, 5 last region
+    };
+
+    // Tile-local exclusive prefix of visible items at tile position q (0..SIZE).
+    __device__ static __forceinline__ uint32_t excl(const Smem& sm, uint32_t q)
+    {
+        if (q >= (uint32_t)SIZE) return sm.info[3];
+        const uint32_t j = q / THREADS, r = q % THREADS, w = r >> 5, l = r & 31u;
+        return sm.prefix[j * NW + w] + __popc(sm.ballot[j][w] & ((1u << l) - 1u));
+    }
+
+    // After all ballots are stored and a __syncthreads(): scan the ballot
+    // counts (warp 0) and locate the regions of the tile's first and last
+    // drawable (warp 1).  Ends with __syncthreads().
+    __device__ static __forceinline__ void scan(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
+                                                uint32_t b, uint32_t n)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (warp == 0) {
+            constexpr int PER = (NC + 31) / 32;
+            uint32_t c[PER];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                const int idx = lane * PER + k;
+                c[k] = idx < NC ? __popc(sm.ballot[idx / NW][idx % NW]) : 0u;
+                sum += c[k];
+            }
+            uint32_t incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(~0u, incl, o);
+                if (lane >= o) incl += v;
+            }
+            uint32_t run = incl - sum;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                const int idx = lane * PER + k;
+                if (idx < NC) sm.prefix[idx] = run;
+                run += c[k];
+            }
+            if (lane == 31) sm.info[3] = incl;
+        } else if (warp == 1 && lane == 0) {
+            // Clamped to S-1 so that an empty scene (n == 0, one work item)
+            // stays inside the offsets and counts arrays.
+            const uint32_t e = min(b + (uint32_t)SIZE, n);
+            sm.info[4] = min(region_of(offsets, 0, S + 1, b), S - 1);
+            sm.info[5] = n ? min(region_of(offsets, 0, S + 1, e - 1), S - 1) : S - 1;
+        }
+        __syncthreads();
+    }
+
+    // Warp 0: publish the tile aggregate, look back, publish the inclusive
+    // prefix.  `item` indexes `states`; items in [first, item) precede it in
+    // the same scan.  Ends with __syncthreads(); carry in info[2].
+    __device__ static __forceinline__ void lookback(Smem& sm, uint64_t* __restrict__ states, int64_t item,
+                                                    int64_t first, const uint32_t* __restrict__ offsets, uint32_t b,
+                                                    uint64_t limit_ns, uint32_t fault, uint32_t* error)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (warp == 0) {
+            const uint32_t total = sm.info[3];
+            const uint32_t epoch = sm.info[1];
+            const uint32_t last_start = __ldg(offsets + sm.info[5]);
+            const uint32_t head = last_start >= b ? 1u : 0u;
+            const uint32_t val = head ? total - excl(sm, last_start - b) : total;
+            uint32_t carry = 0;
+            bool timed_out = false;
+            if (item == first) {
+                if (lane == 0 && fault != CADR_FAULT_SKIP_FIRST_TILE_PUBLISH)
+                    store_relaxed_u64(states + item, pack_status(epoch, kStatusPrefix, 1u, val));
+            } else {
+                if (lane == 0) store_relaxed_u64(states + item, pack_status(epoch, kStatusAgg, head, val));
+                carry = warp_lookback(states, item, first, epoch, limit_ns, timed_out);
+                if (lane == 0)
+                    store_relaxed_u64(states + item, pack_status(epoch, kStatusPrefix, head, head ? val : carry + val));
+            }
+            if (lane == 0) {
+                sm.info[2] = carry;
+                if (timed_out) atomicOr(error, CADR_DEVERR_LOOKBACK_TIMEOUT);
+            }
+        }
+        __syncthreads();
+    }
+
+    // Every thread: write the commands of its visible items and the counts
+    // of the regions ending in this tile (the scan's first tile also writes
+    // the zero counts of empty regions).
+    __device__ static __forceinline__ void write(const Smem& sm, uint32_t vis_bits, uint32_t lod_bits,
+                                                 const uint32_t (&geo)[IPT], uint32_t b, uint32_t n, bool first_tile,
+                                                 const uint32_t* __restrict__ offsets, uint32_t S,
+                                                 const uint4* __restrict__ lods, uint32_t G, uint32_t L,
+                                                 uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts,
+                                                 uint32_t* error)
+    {
+        const int t = threadIdx.x;
+        const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
+        const uint32_t start_f = __ldg(offsets + rf);
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            if (!((vis_bits >> j) & 1u)) continue;
+            const uint32_t i = b + (uint32_t)(j * THREADS + t);
+            const uint32_t r = (rf == rl) ? rf : region_of(offsets, rf, rl + 1, i);
+            const uint32_t start = (r == rf) ? start_f : __ldg(offsets + r);
+            const uint32_t ei = excl(sm, i - b);
+            const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
+            uint32_t g = geo[j];
+            if (g >= G) {
+                atomicOr(error, CADR_DEVERR_BAD_INDEX);
+                g = 0;
+            }
+            const uint4 e = __ldg(lods + (size_t)g * L + ((lod_bits >> (2 * j)) & 3u));
+            uint32_t* c = cmds + (size_t)slot * 5;
+            c[0] = e.x;
+            c[1] = 1u;
+            c[2] = e.y;
+            c[3] = e.z;
+            c[4] = i;
+        }
+        const uint32_t e_tile = min(b + (uint32_t)SIZE, n);
+        for (uint32_t k = rf + (uint32_t)t; k <= rl; k += THREADS) {
+            const uint32_t sk = __ldg(offsets + k), ek = __ldg(offsets + k + 1);
+            if (ek > sk && ek > b && ek <= e_tile) {
+                const uint32_t ee = excl(sm, ek - b);
+                counts[k] = (sk >= b) ? ee - excl(sm, sk - b) : carry + ee;
+            }
+        }
+        if (first_tile)
+            for (uint32_t k = (uint32_t)t; k < S; k += THREADS)
+                if (__ldg(offsets + k) == __ldg(offsets + k + 1)) counts[k] = 0u;
+    }
+};
+
+// Called by thread 0 of every CTA as its last action: the last CTA of the
+// launch re-arms the control block for the next pass.
+__device__ __forceinline__ void finish_pass(LookbackCtl* ctl)
+{
+    __threadfence();
+    const uint32_t old = atomicAdd(&ctl->done_counter, 1u);
+    if (old == gridDim.x - 1) {
+        atomicExch(&ctl->tile_counter, 0u);
+        atomicExch(&ctl->done_counter, 0u);
+        atomicAdd(&ctl->epoch, 1u);
+    }
+}
+
+}  // namespace cadr

@@ -1,0 +1,93 @@
+// kernels.cuh - launch interface between the C ABI layer and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace cadr {
+
+// Scratch of one running pass: lookback control block + tile states.
+struct Scratch {
+    LookbackCtl* ctl = nullptr;
+    uint64_t* tile_state = nullptr;
+    uint64_t capacity = 0;      // tile states available
+    uint64_t launches = 0;      // passes run since the last full reset
+};
+
+struct LeafArgs {
+    const float4* local;          // N * 4 columns
+    const uint32_t* parent;       // N or nullptr (world = local)
+    const float4* parent_world;   // parent level world, 4 columns per node
+    uint32_t num_parents;
+    const float4* sphere;         // N
+    const uint32_t* geometry;     // N
+    const uint32_t* offsets;      // S + 1
+    uint32_t num_state_sets;
+    const uint4* lods;            // G * L
+    uint32_t num_geometries;
+    uint32_t num_lods;
+    uint32_t n;
+    float4* world;                // N * 4 (written)
+    float4* world_sphere;         // N or nullptr (written)
+    uint32_t* cmds;               // N * 5 words
+    uint32_t* counts;             // S
+    uint32_t* marginal;           // ceil(N/32) or nullptr
+    uint32_t* error;              // device-visible error word
+    uint64_t spin_limit_ns;
+    uint32_t fault;
+    ViewConst view;
+};
+
+// Sphere-only cull of one view (batched form): inputs are world spheres.
+struct ViewJob {
+    const float4* world_sphere;
+    const uint32_t* geometry;
+    const uint32_t* offsets;
+    const uint4* lods;
+    uint32_t* cmds;
+    uint32_t* counts;
+    uint32_t* marginal;
+    uint32_t n;
+    uint32_t num_state_sets;
+    uint32_t num_geometries;
+    uint32_t num_lods;
+    uint32_t first_item;          // first global work item of this view
+    uint32_t num_tiles;
+    uint32_t pad[2];
+    ViewConst view;
+};
+
+constexpr int kLeafThreads = 256;
+constexpr int kLeafIpt = 8;
+constexpr int kLeafTile = kLeafThreads * kLeafIpt;
+constexpr int kPropThreads = 256;
+
+// Internal level: world[i] = parent_world[parent[i]] * local[i].
+// staged != 0 asserts non-decreasing parents (bulk copy of the parent run).
+cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, const float4* local,
+                             const uint32_t* parent, uint32_t n, float4* world, int staged,
+                             uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream);
+
+// Leaf level propagation (+ optional world spheres) without culling.
+cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
+
+// Fused plain pass over the leaf level: propagate, transform spheres, cull,
+// select LOD, compact per StateSet.
+cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream);
+
+// Batched sphere cull: one persistent launch over all (view, tile) items.
+cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items,
+                                Scratch& s, uint32_t* error, uint64_t spin_limit_ns,
+                                uint32_t block_threads, uint32_t items_per_thread, uint32_t grid,
+                                cudaStream_t stream);
+uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread);
+
+// Tier A.
+cudaError_t launch_process_drawables(uint32_t level, const uint64_t* root,
+                                     const cadr_drawable_gpu_data* drawables, uint64_t n,
+                                     cadr_draw_indirect_cmd* indirect,
+                                     cadr_drawable_pointers* pointers, cudaStream_t stream);
+
+}  // namespace cadr

@@ -1,0 +1,440 @@
+"""ctypes binding of libcadr_cuda.so (the C ABI declared in include/cadr_cuda.h).
+
+This is the reference-facing call path the tests and the benchmark drive.
+There is no fallback: when the CUDA library is missing, load() raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .scenes import CMD_DTYPE, LOD_DTYPE, Scene
+from .views import VIEW_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libcadr_cuda.so")
+MAX_LEVELS = 16
+
+STATUS = {0: "CADR_OK", 1: "CADR_ERR_INVALID_ARG", 2: "CADR_ERR_OUT_OF_MEMORY", 3: "CADR_ERR_TIMEOUT",
+          4: "CADR_ERR_CUDA", 5: "CADR_ERR_DEVICE", 6: "CADR_ERR_NOT_READY", 7: "CADR_ERR_REJECTED"}
+OK, INVALID_ARG, OUT_OF_MEMORY, TIMEOUT, CUDA, DEVICE, NOT_READY, REJECTED = range(8)
+FAULT_NONE, FAULT_SKIP_FIRST_TILE_PUBLISH = 0, 1
+
+# Exported symbols of the C ABI (checked against include/cadr_cuda.h by the tests).
+vp, u32, u64, i32, sz = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_size_t
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_levels", u32), ("num_state_sets", u32), ("level_size", u64 * MAX_LEVELS),
+                ("num_drawables", u64), ("num_geometries", u32), ("num_lods", u32)]
+
+
+class SceneBuffers(C.Structure):
+    _fields_ = [("level_local", vp * MAX_LEVELS), ("level_parent", vp * MAX_LEVELS),
+                ("level_world", vp * MAX_LEVELS), ("local", vp), ("parent", vp), ("sphere", vp),
+                ("geometry", vp), ("state_set_offsets", vp), ("lods", vp), ("world", vp),
+                ("world_sphere", vp)]
+
+
+class View(C.Structure):
+    _fields_ = [("raw", C.c_uint8 * 144)]
+
+
+class BatchView(C.Structure):
+    _fields_ = [("scene", vp), ("view", View), ("cmds", vp), ("counts", vp), ("marginal", vp)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("block_threads", u32), ("items_per_thread", u32), ("ctas_per_sm", u32),
+                ("reserved", u32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_inflight_batches", u32), ("max_batch_views", u32), ("window_ns", u64),
+                ("memory_budget_bytes", u64), ("reserve_bytes", u64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("request_id", u64), ("status", i32), ("num_views", u32), ("submit_ns", u64),
+                ("complete_ns", u64), ("cmds", vp * 4), ("counts", vp * 4)]
+
+
+class FrameInfo(C.Structure):
+    _fields_ = [("frame", u64), ("propagate_ms", C.c_float), ("leaf_ms", C.c_float), ("total_ms", C.c_float),
+                ("reserved", u32)]
+
+
+_SIGS = {
+    "cadr_status_string": ([i32], C.c_char_p),
+    "cadr_last_error": ([], C.c_char_p),
+    "cadr_abi_version": ([], i32),
+    "cadr_context_create": ([i32, C.POINTER(vp)], i32),
+    "cadr_context_destroy": ([vp], i32),
+    "cadr_context_stream": ([vp], vp),
+    "cadr_context_upload_stream": ([vp], vp),
+    "cadr_context_set_spin_limit_ns": ([vp, u64], i32),
+    "cadr_context_synchronize": ([vp], i32),
+    "cadr_context_launch_count": ([vp], u64),
+    "cadr_context_check_device_error": ([vp, C.POINTER(u32)], i32),
+    "cadr_debug_set_fault": ([vp, u32], i32),
+    "cadr_context_set_collect_frame_info": ([vp, i32], i32),
+    "cadr_context_get_frame_infos": ([vp, C.POINTER(FrameInfo), u32, C.POINTER(u32)], i32),
+    "cadr_device_alloc": ([vp, sz, C.POINTER(vp)], i32),
+    "cadr_device_free": ([vp, vp], i32),
+    "cadr_host_alloc_pinned": ([sz, C.POINTER(vp)], i32),
+    "cadr_host_free_pinned": ([vp], i32),
+    "cadr_upload": ([vp, vp, vp, sz, vp], i32),
+    "cadr_download": ([vp, vp, vp, sz, vp], i32),
+    "cadr_stream_synchronize": ([vp], i32),
+    "cadr_process_drawables": ([vp, u32, vp, vp, u64, vp, vp, vp], i32),
+    "cadr_scene_create": ([vp, C.POINTER(SceneDesc), C.POINTER(vp)], i32),
+    "cadr_scene_destroy": ([vp], i32),
+    "cadr_scene_get_buffers": ([vp, C.POINTER(SceneBuffers)], i32),
+    "cadr_scene_upload_level": ([vp, u32, vp, vp, u64, u64], i32),
+    "cadr_scene_upload_drawables": ([vp, vp, vp, vp, vp, u64, u64], i32),
+    "cadr_scene_upload_state_sets": ([vp, vp], i32),
+    "cadr_scene_upload_lods": ([vp, vp], i32),
+    "cadr_scene_commit": ([vp], i32),
+    "cadr_scene_propagate": ([vp, i32, vp], i32),
+    "cadr_cull": ([vp, vp, vp, vp, vp, vp], i32),
+    "cadr_cull_batched": ([vp, C.POINTER(BatchView), u32, C.POINTER(Tuning), i32, vp], i32),
+    "cadr_autotune_batched": ([vp, C.POINTER(BatchView), u32, u32, C.POINTER(Tuning),
+                               C.POINTER(C.c_float)], i32),
+    "cadr_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+    "cadr_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+    "cadr_server_create": ([vp, C.POINTER(ServerConfig), C.POINTER(vp)], i32),
+    "cadr_server_destroy": ([vp], i32),
+    "cadr_server_submit": ([vp, vp, vp, u32, C.POINTER(u64)], i32),
+    "cadr_server_poll": ([vp, C.POINTER(RequestResult), u32, C.POINTER(u32)], i32),
+    "cadr_server_release": ([vp, u64], i32),
+    "cadr_server_drain": ([vp], i32),
+}
+
+_lib = None
+
+
+class CadrError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree libcadr_cuda.so.  Raises when it has not been built:
+    this package has no CPU fallback."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with cadr_gb300.build.build()")
+        lib = C.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise CadrError(status, load().cadr_last_error().decode())
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, DeviceBuffer):
+        return a.ptr
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a)
+
+
+def view_struct(rec: np.ndarray) -> View:
+    rec = np.ascontiguousarray(rec, VIEW_DTYPE).reshape(-1)
+    v = View()
+    C.memmove(C.addressof(v), rec.ctypes.data, 144)
+    return v
+
+
+class DeviceBuffer:
+    """Device memory owned through cadr_device_alloc / cadr_device_free."""
+
+    def __init__(self, ctx: "Context", nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = vp()
+        check(load().cadr_device_alloc(ctx.handle, self.nbytes, C.byref(p)))
+        self.ptr = p.value or 0
+
+    def free(self):
+        if self.ptr:
+            load().cadr_device_free(self.ctx.handle, self.ptr)
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host memory (cadr_host_alloc_pinned) viewed as numpy."""
+
+    def __init__(self, nbytes: int):
+        p = vp()
+        check(load().cadr_host_alloc_pinned(int(nbytes), C.byref(p)))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+        self.array = np.ctypeslib.as_array((C.c_uint8 * max(1, self.nbytes)).from_address(self.ptr))
+
+    def view(self, dtype, shape):
+        return self.array[: int(np.prod(shape)) * np.dtype(dtype).itemsize].view(dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            load().cadr_host_free_pinned(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = vp()
+        check(self.lib.cadr_context_create(device, C.byref(h)))
+        self.handle = h.value
+
+    def close(self):
+        if self.handle:
+            self.lib.cadr_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self.lib.cadr_context_stream(self.handle) or 0
+
+    def sync(self):
+        check(self.lib.cadr_context_synchronize(self.handle))
+
+    def check_device_error(self) -> int:
+        bits = u32()
+        st = self.lib.cadr_context_check_device_error(self.handle, C.byref(bits))
+        if st != OK:
+            raise CadrError(st, self.lib.cadr_last_error().decode())
+        return bits.value
+
+    def device_error_status(self):
+        bits = u32()
+        st = self.lib.cadr_context_check_device_error(self.handle, C.byref(bits))
+        return st, bits.value
+
+    def set_spin_limit_ns(self, ns: int):
+        check(self.lib.cadr_context_set_spin_limit_ns(self.handle, int(ns)))
+
+    def set_fault(self, fault: int):
+        check(self.lib.cadr_debug_set_fault(self.handle, fault))
+
+    def collect_frame_info(self, on: bool):
+        check(self.lib.cadr_context_set_collect_frame_info(self.handle, 1 if on else 0))
+
+    def frame_infos(self):
+        buf = (FrameInfo * 256)()
+        n = u32()
+        out = []
+        while True:
+            check(self.lib.cadr_context_get_frame_infos(self.handle, buf, 256, C.byref(n)))
+            out += [(buf[i].propagate_ms, buf[i].leaf_ms, buf[i].total_ms) for i in range(n.value)]
+            if n.value < 256:
+                return out
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.cadr_context_launch_count(self.handle))
+
+    def alloc(self, nbytes: int) -> DeviceBuffer:
+        return DeviceBuffer(self, nbytes)
+
+    def upload(self, dst, src: np.ndarray, stream=None):
+        src = np.ascontiguousarray(src)
+        check(self.lib.cadr_upload(self.handle, _ptr(dst), src.ctypes.data, src.nbytes, stream))
+
+    def to_device(self, src: np.ndarray) -> DeviceBuffer:
+        src = np.ascontiguousarray(src)
+        b = self.alloc(max(16, src.nbytes))
+        self.upload(b, src)
+        self.sync()
+        return b
+
+    def download(self, src, dtype, shape, stream=None) -> np.ndarray:
+        out = np.empty(shape, dtype)
+        check(self.lib.cadr_download(self.handle, out.ctypes.data, _ptr(src), out.nbytes, stream))
+        check(self.lib.cadr_stream_synchronize(stream or self.stream))
+        return out
+
+    def process_drawables(self, level: int, root: int, drawables, n: int, indirect, pointers, stream=None):
+        check(self.lib.cadr_process_drawables(self.handle, level, root, _ptr(drawables), n,
+                                              _ptr(indirect), _ptr(pointers), stream))
+
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        check(self.lib.cadr_get_tuning(self.handle, C.byref(t)))
+        return t
+
+    def set_tuning(self, block_threads, items_per_thread, ctas_per_sm):
+        t = Tuning(block_threads, items_per_thread, ctas_per_sm, 0)
+        check(self.lib.cadr_set_tuning(self.handle, C.byref(t)))
+
+
+class CullOutputs:
+    """Device output buffers of one view of one scene."""
+
+    def __init__(self, ctx: Context, n: int, num_state_sets: int, marginal: bool = True):
+        self.n, self.S = n, num_state_sets
+        self.cmds = ctx.alloc(max(16, n * 20))
+        self.counts = ctx.alloc(max(16, num_state_sets * 4))
+        self.marginal = ctx.alloc(max(16, ((n + 31) // 32) * 4)) if marginal else None
+        self.ctx = ctx
+
+    def fetch(self, stream=None) -> dict:
+        counts = self.ctx.download(self.counts, np.uint32, (self.S,), stream)
+        cmds = self.ctx.download(self.cmds, CMD_DTYPE, (self.n,), stream)
+        out = {"counts": counts, "cmds": cmds}
+        if self.marginal is not None:
+            out["marginal"] = self.ctx.download(self.marginal, np.uint32, ((self.n + 31) // 32,), stream)
+        return out
+
+
+class DeviceScene:
+    """A cadr_scene created from a host Scene (scenes.Scene)."""
+
+    def __init__(self, ctx: Context, scene: Scene, upload: bool = True):
+        self.ctx, self.host = ctx, scene
+        d = SceneDesc()
+        d.num_levels = len(scene.level_local)
+        d.num_state_sets = scene.num_state_sets
+        for l, a in enumerate(scene.level_local):
+            d.level_size[l] = a.shape[0]
+        d.num_drawables = scene.n
+        d.num_geometries = scene.num_geometries
+        d.num_lods = scene.num_lods
+        h = vp()
+        check(ctx.lib.cadr_scene_create(ctx.handle, C.byref(d), C.byref(h)))
+        self.handle = h.value
+        if upload:
+            self.upload_all()
+
+    def upload_all(self):
+        s, L = self.host, self.ctx.lib
+        for l, (loc, par) in enumerate(zip(s.level_local, s.level_parent)):
+            check(L.cadr_scene_upload_level(self.handle, l, _ptr(np.ascontiguousarray(loc)),
+                                            _ptr(None if par is None else np.ascontiguousarray(par)),
+                                            0, loc.shape[0]))
+        check(L.cadr_scene_upload_drawables(self.handle, _ptr(s.local), _ptr(s.parent), _ptr(s.sphere),
+                                            _ptr(s.geometry), 0, s.n))
+        check(L.cadr_scene_upload_state_sets(self.handle, _ptr(s.state_set_offsets)))
+        check(L.cadr_scene_upload_lods(self.handle, _ptr(np.ascontiguousarray(s.lods, LOD_DTYPE))))
+        check(L.cadr_scene_commit(self.handle))
+
+    def buffers(self) -> SceneBuffers:
+        b = SceneBuffers()
+        check(self.ctx.lib.cadr_scene_get_buffers(self.handle, C.byref(b)))
+        return b
+
+    def propagate(self, world_spheres: bool = True, stream=None):
+        check(self.ctx.lib.cadr_scene_propagate(self.handle, 1 if world_spheres else 0, stream))
+
+    def cull(self, view: np.ndarray, out: CullOutputs, stream=None):
+        v = np.ascontiguousarray(view, VIEW_DTYPE)
+        check(self.ctx.lib.cadr_cull(self.handle, v.ctypes.data, out.cmds.ptr, out.counts.ptr,
+                                     out.marginal.ptr if out.marginal is not None else None, stream))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.cadr_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_views(items) -> C.Array:
+    """items: iterable of (DeviceScene, view record, CullOutputs)."""
+    items = list(items)
+    arr = (BatchView * len(items))()
+    for k, (ds, view, out) in enumerate(items):
+        arr[k].scene = ds.handle
+        arr[k].view = view_struct(view)
+        arr[k].cmds = out.cmds.ptr
+        arr[k].counts = out.counts.ptr
+        arr[k].marginal = out.marginal.ptr if out.marginal is not None else None
+    return arr
+
+
+def cull_batched(ctx: Context, arr, tuning: Tuning | None = None, use_graph: bool = True, stream=None):
+    check(ctx.lib.cadr_cull_batched(ctx.handle, arr, len(arr), C.byref(tuning) if tuning else None,
+                                    1 if use_graph else 0, stream))
+
+
+def autotune_batched(ctx: Context, arr, reps: int = 5):
+    t = Tuning()
+    ms = C.c_float()
+    check(ctx.lib.cadr_autotune_batched(ctx.handle, arr, len(arr), reps, C.byref(t), C.byref(ms)))
+    return t, ms.value
+
+
+class Server:
+    def __init__(self, ctx: Context, max_inflight: int = 4, max_batch_views: int = 64,
+                 window_ns: int = 200_000, memory_budget: int = 0, reserve: int = 0):
+        self.ctx = ctx
+        cfg = ServerConfig(max_inflight, max_batch_views, window_ns, memory_budget, reserve)
+        h = vp()
+        check(ctx.lib.cadr_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+        self._res = (RequestResult * 256)()
+
+    def submit(self, scene: DeviceScene, views: np.ndarray) -> int:
+        v = np.ascontiguousarray(views, VIEW_DTYPE).reshape(-1)
+        rid = u64()
+        check(self.ctx.lib.cadr_server_submit(self.handle, scene.handle, v.ctypes.data, v.shape[0],
+                                              C.byref(rid)))
+        return rid.value
+
+    def poll(self):
+        n = u32()
+        check(self.ctx.lib.cadr_server_poll(self.handle, self._res, 256, C.byref(n)))
+        return [self._res[i] for i in range(n.value)]
+
+    def release(self, rid: int):
+        check(self.ctx.lib.cadr_server_release(self.handle, rid))
+
+    def drain(self):
+        check(self.ctx.lib.cadr_server_drain(self.handle))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.cadr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

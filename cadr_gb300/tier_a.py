@@ -1,0 +1,143 @@
+"""Synthetic CadR device-memory images for the Tier A pass.
+
+An image is the bytes of one device buffer at a known base address holding
+everything the processDrawables pass dereferences:
+  * the handle table, laid out exactly as src/CadR/HandleTable.cpp grows it:
+    handles start at 1 (0 is invalid), 2048 entries per table, one level up
+    to handle 2047, two levels up to 2048^2 - 1, three beyond
+    (createHandle1..3, HandleTable.cpp:142-337);
+  * PrimitiveSet arrays {uint32 count, uint32 first} (PrimitiveSet.h:12-15),
+    one array per Geometry;
+  * MatrixList allocations: a 64-byte header {numMatrices, capacity, 0...}
+    followed by the matrices (MatrixList.h:54-59).
+Vertex, index and drawable-data allocations are only resolved by the pass,
+never read, so their addresses point into a second region that the image
+does not hold.
+
+Drawables are packed in the StateSet depth-first order of
+StateSet::recordToCommandBuffer (StateSet.cpp:198-262): a root StateSet with
+`num_state_sets` children, drawables grouped by child in child order.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import rng
+
+DRAWABLE_DTYPE = np.dtype([("vertex_data_handle", np.uint64), ("index_data_handle", np.uint64),
+                           ("matrix_list_handle", np.uint64), ("drawable_data_handle", np.uint64),
+                           ("primitive_set_handle", np.uint64), ("primitive_set_offset", np.uint32),
+                           ("padding", np.uint32)])
+assert DRAWABLE_DTYPE.itemsize == 48
+
+TABLE = 2048
+
+
+def handle_level(highest_handle: int) -> int:
+    """Table depth after creating handles 1..highest_handle (HandleTable.cpp)."""
+    if highest_handle <= TABLE - 1:
+        return 1
+    if highest_handle <= TABLE * TABLE - 1:
+        return 2
+    return 3
+
+
+@dataclass
+class TierAImage:
+    image: np.ndarray          # uint8, device bytes at `base`
+    base: int
+    level: int
+    root: int                  # device address of the root table
+    drawables: np.ndarray      # DRAWABLE_DTYPE [N], StateSet DFS order
+    state_set_counts: np.ndarray  # drawables per StateSet (DFS order of the regions)
+    num_handles: int
+
+
+def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries: int | None = None,
+          prims_per_geometry: int = 3, with_drawable_data: bool = True,
+          matrices_per_list: int = 1, extra_handles: int = 0) -> TierAImage:
+    """Builds the image of n drawables.  base must be 256-byte aligned; it is
+    the device address the image will be uploaded to."""
+    assert base % 256 == 0
+    G = num_geometries or max(1, min(n, 4096))
+    idx = np.arange(max(n, 1), dtype=np.uint64)[:n]
+    # Handle creation order: per geometry (vertex, index, primitiveSets),
+    # then one MatrixList per drawable, then one drawable-data allocation
+    # per drawable, then `extra_handles` unused handles.
+    h_vertex = 1 + 3 * np.arange(G, dtype=np.uint64)
+    h_index = h_vertex + 1
+    h_prims = h_vertex + 2
+    h_ml = 1 + 3 * G + np.arange(n, dtype=np.uint64)
+    h_dd = (1 + 3 * G + n + np.arange(n, dtype=np.uint64)) if with_drawable_data else np.zeros(n, np.uint64)
+    H = 3 * G + n + (n if with_drawable_data else 0) + extra_handles
+    level = handle_level(H)
+
+    # Region sizes.
+    n_llt = H // TABLE + 1                      # last-level tables
+    n_rt = 0 if level < 3 else (H >> 22) + 1    # level-1 routing tables (level 3 only)
+    n_tables = n_llt + (1 if level == 2 else 0) + (n_rt + 1 if level == 3 else 0)
+    tables_bytes = n_tables * TABLE * 8
+    prims_off = tables_bytes
+    prims_bytes = G * prims_per_geometry * 8
+    ml_stride = 64 + 64 * matrices_per_list
+    ml_off = (prims_off + prims_bytes + 255) & ~255
+    size = ml_off + n * ml_stride
+    img = np.zeros(size, np.uint8)
+    tables = img[:tables_bytes].view(np.uint64).reshape(n_tables, TABLE)
+
+    # Addresses of every handle's target.
+    addr = np.zeros(H + 1, np.uint64)
+    far = np.uint64(base + ((size + (1 << 20)) & ~((1 << 20) - 1)))  # unbacked region
+    addr[h_vertex.astype(np.int64)] = far + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
+    addr[h_index.astype(np.int64)] = far + np.uint64(G << 16) + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
+    addr[h_prims.astype(np.int64)] = np.uint64(base + prims_off) + np.arange(G, dtype=np.uint64) * np.uint64(prims_per_geometry * 8)
+    addr[h_ml.astype(np.int64)] = np.uint64(base + ml_off) + idx * np.uint64(ml_stride)
+    if with_drawable_data:
+        addr[h_dd.astype(np.int64)] = far + np.uint64(2 * G << 16) + idx * np.uint64(256)
+
+    # Last-level tables: llt k holds handles [k*2048, k*2048 + 2047].
+    llt = tables[:n_llt].reshape(-1)
+    llt[: H + 1] = addr
+    llt_addr = np.uint64(base) + np.arange(n_llt, dtype=np.uint64) * np.uint64(TABLE * 8)
+    if level == 1:
+        root = base
+    elif level == 2:
+        rt = tables[n_llt]
+        rt[:n_llt] = llt_addr
+        root = base + n_llt * TABLE * 8
+    else:
+        # Routing tables m (handles with h >> 22 == m), then the level-2 root.
+        for m in range(n_rt):
+            lo, hi = m * TABLE, min((m + 1) * TABLE, n_llt)
+            tables[n_llt + m, : hi - lo] = llt_addr[lo:hi]
+        rt_addr = np.uint64(base) + (n_llt + np.arange(n_rt, dtype=np.uint64)) * np.uint64(TABLE * 8)
+        tables[n_llt + n_rt, :n_rt] = rt_addr
+        root = base + (n_llt + n_rt) * TABLE * 8
+
+    # PrimitiveSets and MatrixList headers.
+    ps = img[prims_off:prims_off + prims_bytes].view(np.uint32).reshape(G, prims_per_geometry, 2)
+    st = rng.Stream(seed, "tierA.prims")
+    cnt = st.integers(np.arange(G * prims_per_geometry, dtype=np.uint64), 36, 3000).reshape(G, prims_per_geometry)
+    ps[:, :, 0] = cnt
+    ps[:, :, 1] = np.cumsum(cnt.reshape(-1)).reshape(G, prims_per_geometry) - cnt
+    mlh = img[ml_off:ml_off + n * ml_stride].view(np.uint32).reshape(n, ml_stride // 4)
+    mlh[:, 0] = matrices_per_list
+    mlh[:, 1] = matrices_per_list
+
+    # Drawable records, grouped by StateSet (DFS order of the children).
+    g_of = rng.Stream(seed, "tierA.geometry").integers(idx, 0, G - 1)
+    p_of = rng.Stream(seed, "tierA.prim").integers(idx, 0, prims_per_geometry - 1)
+    ss = rng.Stream(seed, "tierA.stateset").integers(idx, 0, num_state_sets - 1)
+    order = np.argsort(ss, kind="stable")
+    d = np.zeros(n, DRAWABLE_DTYPE)
+    d["vertex_data_handle"] = h_vertex[g_of]
+    d["index_data_handle"] = h_index[g_of]
+    d["matrix_list_handle"] = h_ml
+    d["drawable_data_handle"] = h_dd
+    d["primitive_set_handle"] = h_prims[g_of]
+    d["primitive_set_offset"] = (p_of * 8).astype(np.uint32)
+    d = d[order]
+    counts = np.bincount(ss, minlength=num_state_sets).astype(np.uint32)
+    return TierAImage(img, base, level, int(root), np.ascontiguousarray(d), counts, H)

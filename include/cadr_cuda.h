@@ -1,0 +1,354 @@
+/*
+ * cadr_cuda.h - C ABI of the GB300 (sm_103a) drawable-processing pass.
+ *
+ * Every entry point takes plain pointers and sizes.  Device buffers are raw
+ * device pointers (the CUDA equivalent of a VkDeviceAddress); streams are
+ * cudaStream_t values passed as `void*` (NULL = the context's own stream).
+ * No C++ exception crosses this boundary: every call returns a cadr_status,
+ * and cadr_last_error() gives a one-line description of the last failure on
+ * the calling thread.
+ *
+ * Two tiers share one context:
+ *   Tier A  cadr_process_drawables: the handle-resolution pass of the
+ *           reference's processDrawables compute shader, bit-exact.
+ *   Tier B  cadr_cull / cadr_cull_batched / cadr_server_*: hierarchy
+ *           propagation, bounding-sphere frustum culling with screen-size LOD
+ *           selection and deterministic per-StateSet compaction into
+ *           VkDrawIndexedIndirectCommand records.
+ *
+ * Reference interfaces replaced (paths inside the CADR project):
+ *   src/CadR/Renderer.cpp:598-720   Renderer::recordDrawableProcessing
+ *   src/CadR/shaders/processDrawables.comp:68-113  push constants + main()
+ *   src/CadR/StateSet.cpp:198-268   per-StateSet regions and draw counts
+ *   src/CadR/Renderer.cpp:946-999   Renderer::executeCopyOperations (uploads)
+ */
+#ifndef CADR_CUDA_H
+#define CADR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define CADR_API __declspec(dllexport)
+#else
+#define CADR_API __attribute__((visibility("default")))
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  They mirror the reference's exception classes
+ * (src/CadR/Exceptions.h:13-40): OUT_OF_MEMORY <-> CadR::OutOfResources,
+ * TIMEOUT <-> CadR::Timeout, INVALID_ARG <-> CadR::LogicError.            */
+typedef enum cadr_status {
+    CADR_OK = 0,
+    CADR_ERR_INVALID_ARG = 1,
+    CADR_ERR_OUT_OF_MEMORY = 2,
+    CADR_ERR_TIMEOUT = 3,      /* a bounded device wait expired (lookback, mbarrier) */
+    CADR_ERR_CUDA = 4,         /* a CUDA runtime call failed */
+    CADR_ERR_DEVICE = 5,       /* a kernel reported an error through its error word */
+    CADR_ERR_NOT_READY = 6,    /* polled work has not finished yet */
+    CADR_ERR_REJECTED = 7      /* serving admission refused the request */
+} cadr_status;
+
+/* Device error word bits (read back by the host after a pass). */
+#define CADR_DEVERR_LOOKBACK_TIMEOUT 0x1u
+#define CADR_DEVERR_MBARRIER_TIMEOUT 0x2u
+#define CADR_DEVERR_BAD_INDEX 0x4u
+
+typedef void* cadr_stream; /* cudaStream_t */
+typedef struct cadr_context cadr_context;
+typedef struct cadr_scene cadr_scene;
+typedef struct cadr_server cadr_server;
+
+/* Output record layouts.  They are the Vulkan structs of the same name
+ * (vulkan_core.h), restated so callers need no Vulkan headers. */
+typedef struct cadr_draw_indirect_cmd { /* VkDrawIndirectCommand, 16 B */
+    uint32_t vertex_count;
+    uint32_t instance_count;
+    uint32_t first_vertex;
+    uint32_t first_instance;
+} cadr_draw_indirect_cmd;
+
+typedef struct cadr_draw_indexed_cmd { /* VkDrawIndexedIndirectCommand, 20 B */
+    uint32_t index_count;
+    uint32_t instance_count;
+    uint32_t first_index;
+    int32_t vertex_offset;
+    uint32_t first_instance;
+} cadr_draw_indexed_cmd;
+
+/* Tier A input record: CadR::DrawableGpuData, 48 B (src/CadR/Drawable.h:32-43). */
+typedef struct cadr_drawable_gpu_data {
+    uint64_t vertex_data_handle;
+    uint64_t index_data_handle;
+    uint64_t matrix_list_handle;
+    uint64_t drawable_data_handle;
+    uint64_t primitive_set_handle;
+    uint32_t primitive_set_offset;
+    uint32_t padding;
+} cadr_drawable_gpu_data;
+
+/* Tier A second output: the 32 B DrawablePointers record
+ * (src/CadR/shaders/processDrawables.comp:52-59, Renderer.h:201). */
+typedef struct cadr_drawable_pointers {
+    uint64_t vertex_data_ptr;
+    uint64_t index_data_ptr;
+    uint64_t matrix_list_ptr;
+    uint64_t drawable_data_ptr;
+} cadr_drawable_pointers;
+
+/* One LOD of a geometry: the PrimitiveSet {indexCount, startIndex}
+ * (src/CadR/PrimitiveSet.h:12-15) plus the vertex offset of an indexed draw.
+ * Padded to 16 B so one vector load fetches it. */
+typedef struct cadr_lod {
+    uint32_t index_count;
+    uint32_t first_index;
+    int32_t vertex_offset;
+    uint32_t reserved;
+} cadr_lod;
+
+/* One view (camera or shadow cascade), precomputed on the host.
+ *   planes[p] = (nx, ny, nz, d): a sphere (c, r) is outside plane p when
+ *               ((nx*cx + ny*cy) + nz*cz) + d < -r.
+ *   view_z    = row 2 of the view matrix: z_view = ((vz0*cx + vz1*cy) + vz2*cz) + vz3.
+ *   LOD:      zc = perspective ? max(-z_view, near_z) : 1;  s = r * lod_scale;
+ *             lod = first k < num_lods-1 with s >= lod_threshold[k] * zc,
+ *                   else num_lods-1.                                      */
+typedef struct cadr_view {
+    float planes[6][4];
+    float view_z[4];
+    float lod_threshold[4];
+    float lod_scale;
+    float near_z;
+    uint32_t perspective;
+    uint32_t reserved;
+} cadr_view; /* 144 B */
+
+#define CADR_MAX_LEVELS 16
+
+/* Shape of a Tier B scene: internal hierarchy levels 0..num_levels-1 followed
+ * by the leaf level, which holds one world matrix per drawable.  Drawables
+ * are stored grouped by StateSet, StateSet s owning the contiguous range
+ * [state_set_offsets[s], state_set_offsets[s+1]) (src/CadR/StateSet.h:47,
+ * StateSet.cpp:233-261). */
+typedef struct cadr_scene_desc {
+    uint32_t num_levels;                 /* internal levels, 0..CADR_MAX_LEVELS */
+    uint32_t num_state_sets;             /* >= 1 */
+    uint64_t level_size[CADR_MAX_LEVELS];
+    uint64_t num_drawables;              /* < 2^32 */
+    uint32_t num_geometries;             /* >= 1 */
+    uint32_t num_lods;                   /* 1..4 */
+} cadr_scene_desc;
+
+/* Device-resident buffers of a scene, for callers that fill or read them in
+ * place (all pointers are device pointers owned by the scene). */
+typedef struct cadr_scene_buffers {
+    float* level_local[CADR_MAX_LEVELS];    /* n*16 floats, column-major mat4 */
+    uint32_t* level_parent[CADR_MAX_LEVELS];/* n (level 0: NULL) */
+    float* level_world[CADR_MAX_LEVELS];    /* n*16 floats (level 0 aliases level_local[0]) */
+    float* local;                           /* N*16 */
+    uint32_t* parent;                       /* N (NULL when num_levels == 0) */
+    float* sphere;                          /* N*4 local bounding spheres (cx,cy,cz,r) */
+    uint32_t* geometry;                     /* N geometry index per drawable */
+    uint32_t* state_set_offsets;            /* S+1 */
+    cadr_lod* lods;                         /* G*num_lods */
+    float* world;                           /* N*16 world matrices (written by passes) */
+    float* world_sphere;                    /* N*4 world bounding spheres (written by passes) */
+} cadr_scene_buffers;
+
+/* ------------------------------------------------------------------------ */
+/* Errors and context. */
+CADR_API const char* cadr_status_string(cadr_status s);
+CADR_API const char* cadr_last_error(void);
+CADR_API int cadr_abi_version(void);
+
+/* Creates the per-device context: streams (compute + upload), pinned staging
+ * ring and lookback scratch.  Replaces the Vulkan device/queue the reference
+ * Renderer is constructed with (src/CadR/Renderer.h:124-128). */
+CADR_API cadr_status cadr_context_create(int device, cadr_context** out);
+CADR_API cadr_status cadr_context_destroy(cadr_context* ctx);
+CADR_API cadr_stream cadr_context_stream(cadr_context* ctx);
+CADR_API cadr_stream cadr_context_upload_stream(cadr_context* ctx);
+/* Upper bound of every bounded device spin, in nanoseconds (default 1e9). */
+CADR_API cadr_status cadr_context_set_spin_limit_ns(cadr_context* ctx, uint64_t ns);
+CADR_API cadr_status cadr_context_synchronize(cadr_context* ctx);
+/* Number of kernels this library launched through ctx since creation. */
+CADR_API uint64_t cadr_context_launch_count(cadr_context* ctx);
+
+/* Device memory helpers (stream-ordered pool of the context's device). */
+CADR_API cadr_status cadr_device_alloc(cadr_context* ctx, size_t bytes, void** out);
+CADR_API cadr_status cadr_device_free(cadr_context* ctx, void* ptr);
+CADR_API cadr_status cadr_host_alloc_pinned(size_t bytes, void** out);
+CADR_API cadr_status cadr_host_free_pinned(void* ptr);
+/* Stream-ordered copies.  Host sources that are not pinned are staged
+ * through the context's pinned ring on the upload stream, which then hands
+ * over to `stream` with an event (replaces DataStorage::recordUploads +
+ * Renderer::executeCopyOperations, src/CadR/DataStorage.cpp:230-281,
+ * Renderer.cpp:946-999, without the 1.5 s fence wait). */
+CADR_API cadr_status cadr_upload(cadr_context* ctx, void* dst_device, const void* src_host,
+                                 size_t bytes, cadr_stream stream);
+CADR_API cadr_status cadr_download(cadr_context* ctx, void* dst_host, const void* src_device,
+                                   size_t bytes, cadr_stream stream);
+CADR_API cadr_status cadr_stream_synchronize(cadr_stream stream);
+
+/* ------------------------------------------------------------------------ */
+/* Tier A.  Replaces Renderer::recordDrawableProcessing
+ * (src/CadR/Renderer.cpp:598-720) and processDrawables.comp:92-113.
+ * For every i < num_drawables (records already packed in StateSet
+ * depth-first order, StateSet.cpp:198-262):
+ *   ps = lookup(d.primitive_set_handle) + d.primitive_set_offset
+ *   ml = lookup(d.matrix_list_handle)
+ *   indirect[i] = {ps->count, ml->numMatrices, ps->first, 0}
+ *   pointers[i] = {lookup(vertex), lookup(index), ml, lookup(drawableData)}
+ * with lookup() the 1/2/3-level handle table walk of
+ * processDrawables.comp:77-89 (handle_level 1..3).  Handles must be valid,
+ * exactly as in the reference. */
+CADR_API cadr_status cadr_process_drawables(cadr_context* ctx, uint32_t handle_level,
+                                            const void* handle_table,
+                                            const cadr_drawable_gpu_data* drawables,
+                                            uint64_t num_drawables,
+                                            cadr_draw_indirect_cmd* indirect,
+                                            cadr_drawable_pointers* pointers,
+                                            cadr_stream stream);
+
+/* ------------------------------------------------------------------------ */
+/* Tier B scenes. */
+CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc* desc,
+                                       cadr_scene** out);
+CADR_API cadr_status cadr_scene_destroy(cadr_scene* scene);
+CADR_API cadr_status cadr_scene_get_buffers(cadr_scene* scene, cadr_scene_buffers* out);
+/* Host uploads of scene inputs (rows [first, first+count) of one array).
+ * `parent` may be NULL to leave the parent array untouched. */
+CADR_API cadr_status cadr_scene_upload_level(cadr_scene* scene, uint32_t level,
+                                             const float* local, const uint32_t* parent,
+                                             uint64_t first, uint64_t count);
+CADR_API cadr_status cadr_scene_upload_drawables(cadr_scene* scene, const float* local,
+                                                 const uint32_t* parent, const float* sphere,
+                                                 const uint32_t* geometry, uint64_t first,
+                                                 uint64_t count);
+CADR_API cadr_status cadr_scene_upload_state_sets(cadr_scene* scene, const uint32_t* offsets);
+CADR_API cadr_status cadr_scene_upload_lods(cadr_scene* scene, const cadr_lod* lods);
+/* Re-validates the scene after in-place device writes (parents monotone?
+ * offsets sorted?) and orders uploads before the next pass. */
+CADR_API cadr_status cadr_scene_commit(cadr_scene* scene);
+
+/* Propagates the internal hierarchy levels (level l world =
+ * level l-1 world[parent] * local, level by level) and, when
+ * write_world_spheres is set, the leaf world matrices and world spheres that
+ * cadr_cull_batched consumes. */
+CADR_API cadr_status cadr_scene_propagate(cadr_scene* scene, int write_world_spheres,
+                                          cadr_stream stream);
+
+/* Plain pass: propagation of every level, then one fused leaf kernel that
+ * computes world matrices, transforms the bounding spheres
+ * (src/CadR/BoundingSphere.h:70-86), culls them against the 6 planes,
+ * selects the LOD and compacts visible drawables of StateSet s into
+ * cmds[offsets[s] .. offsets[s]+counts[s]) in ascending drawable order.
+ * cmds: N records; counts: S words; marginal: optional ceil(N/32) words, bit i
+ * set when drawable i lies within the tolerance band of a plane. */
+CADR_API cadr_status cadr_cull(cadr_scene* scene, const cadr_view* view,
+                               cadr_draw_indexed_cmd* cmds, uint32_t* counts,
+                               uint32_t* marginal, cadr_stream stream);
+
+/* Batched form: many (scene, view) pairs culled by one persistent launch over
+ * (view, tile) work items, replayed from a captured CUDA graph when the
+ * same batch shape repeats.  Scenes must have been propagated with
+ * write_world_spheres = 1. */
+typedef struct cadr_batch_view {
+    cadr_scene* scene;
+    cadr_view view;
+    cadr_draw_indexed_cmd* cmds;  /* device, scene N records */
+    uint32_t* counts;             /* device, scene S words */
+    uint32_t* marginal;           /* device or NULL */
+} cadr_batch_view;
+
+typedef struct cadr_tuning {
+    uint32_t block_threads;       /* 128, 256, 512 */
+    uint32_t items_per_thread;    /* 1..16 */
+    uint32_t ctas_per_sm;         /* persistent grid = ctas_per_sm * SMs */
+    uint32_t reserved;
+} cadr_tuning;
+
+CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view* views,
+                                       uint32_t num_views, const cadr_tuning* tuning,
+                                       int use_graph, cadr_stream stream);
+/* Autotuner: times every supported tuning on this batch (CUDA events, median
+ * of `reps` runs) and keeps the fastest as the context's default. */
+CADR_API cadr_status cadr_autotune_batched(cadr_context* ctx, const cadr_batch_view* views,
+                                           uint32_t num_views, uint32_t reps, cadr_tuning* best,
+                                           float* best_ms);
+CADR_API cadr_status cadr_get_tuning(cadr_context* ctx, cadr_tuning* out);
+CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* tuning);
+
+/* Frame timing, the CUDA counterpart of CadR::FrameInfo's GPU timestamps
+ * (src/CadR/FrameInfo.h:15-31, collected in Renderer.cpp:600-702): while
+ * collection is on, every plain pass records events before propagation,
+ * between propagation and the fused leaf kernel, and after it, into a ring
+ * of 256 frames.  get_frame_infos waits for and returns the frames finished
+ * since the previous call. */
+typedef struct cadr_frame_info {
+    uint64_t frame;
+    float propagate_ms;     /* internal hierarchy levels */
+    float leaf_ms;          /* fused leaf kernel (propagate, cull, LOD, compact) */
+    float total_ms;
+    uint32_t reserved;
+} cadr_frame_info;
+CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int on);
+CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_info* out,
+                                                  uint32_t max_frames, uint32_t* num_frames);
+
+/* Host-side check of the last pass's device error word (0 = no error). */
+CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t* error_bits);
+
+/* Fault injection for the bounded-wait tests: while set, the first tile of
+ * every plain pass never publishes its lookback status, so its successors'
+ * waits run into the spin limit and cadr_context_check_device_error returns
+ * CADR_ERR_TIMEOUT.  The pass still ends; the context stays usable. */
+#define CADR_FAULT_NONE 0u
+#define CADR_FAULT_SKIP_FIRST_TILE_PUBLISH 1u
+CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault);
+
+/* ------------------------------------------------------------------------ */
+/* Serving form: a request loop over resident scenes with continuous
+ * batching.  Requests are admitted as output memory and slots free up;
+ * admitted requests are batched within a window and culled by the batched
+ * kernel on one of several streams, so batches overlap on the device. */
+typedef struct cadr_server_config {
+    uint32_t max_inflight_batches; /* streams in rotation, >= 1 */
+    uint32_t max_batch_views;      /* views per batch */
+    uint64_t window_ns;            /* batching window, e.g. 200000 */
+    uint64_t memory_budget_bytes;  /* output memory the server may hold (0 = from free memory) */
+    uint64_t reserve_bytes;        /* free device memory left untouched */
+} cadr_server_config;
+
+typedef struct cadr_request_result {
+    uint64_t request_id;
+    cadr_status status;
+    uint32_t num_views;
+    uint64_t submit_ns;            /* host monotonic clock */
+    uint64_t complete_ns;
+    const cadr_draw_indexed_cmd* cmds[4]; /* device pointers, valid until released */
+    const uint32_t* counts[4];
+} cadr_request_result;
+
+CADR_API cadr_status cadr_server_create(cadr_context* ctx, const cadr_server_config* cfg,
+                                        cadr_server** out);
+CADR_API cadr_status cadr_server_destroy(cadr_server* srv);
+CADR_API cadr_status cadr_server_submit(cadr_server* srv, cadr_scene* scene,
+                                        const cadr_view* views, uint32_t num_views,
+                                        uint64_t* request_id);
+/* Returns up to max_results finished requests (CADR_OK with *num_results 0
+ * when none finished). */
+CADR_API cadr_status cadr_server_poll(cadr_server* srv, cadr_request_result* results,
+                                      uint32_t max_results, uint32_t* num_results);
+CADR_API cadr_status cadr_server_release(cadr_server* srv, uint64_t request_id);
+CADR_API cadr_status cadr_server_drain(cadr_server* srv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CADR_CUDA_H */

@@ -1,0 +1,161 @@
+"""ctypes binding of oracle/_build/libcadr_oracle.so and oracle/_ref/libcadr_ref.so.
+
+TEST INFRASTRUCTURE ONLY (see oracle/__init__.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcadr_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libcadr_ref.so")
+REFERENCE_ROOT = "/root/reference"
+
+_lib = None
+_ref = None
+
+
+def build(with_ref: bool = True) -> None:
+    """Compiles the oracle (and, when the CADR sources are present, the
+    reference shim) with oracle/Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if with_ref and os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "CadR")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_ROOT}"], check=True)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleLib:
+    def __init__(self, path: str):
+        self.lib = C.CDLL(path)
+        L = self.lib
+        vp, u64, u32, i32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int
+        L.oracle_process_drawables.argtypes = [vp, u64, u64, u32, u64, vp, u64, vp, vp, i32]
+        L.oracle_process_drawables.restype = i32
+        L.oracle_mat4_mul.argtypes = [vp, vp, vp]
+        L.oracle_sphere_transform.argtypes = [vp, vp, vp]
+        L.oracle_cull.argtypes = [u32, vp, vp, vp, u64, vp, vp, vp, vp, u32, vp, u32, u32, vp, vp,
+                                  vp, vp, vp, vp, vp, i32]
+        L.oracle_cull.restype = i32
+        L.oracle_cull_spheres.argtypes = [u64, vp, vp, u32, vp, u32, u32, vp, vp, vp, vp, vp, i32]
+        L.oracle_cull_spheres.restype = i32
+        L.oracle_max_threads.restype = i32
+
+
+def load() -> OracleLib:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(with_ref=False)
+        _lib = OracleLib(LIB_PATH)
+    return _lib
+
+
+def load_ref():
+    """The reference-math shim, or None when it was not built (it needs the
+    CADR sources, which only the build container has)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        _ref = C.CDLL(REF_PATH)
+        _ref.ref_mat4_mul.argtypes = [C.c_void_p] * 3
+        _ref.ref_sphere_transform.argtypes = [C.c_void_p] * 3
+        _ref.ref_glm_version.restype = C.c_int
+    return _ref
+
+
+def max_threads() -> int:
+    return load().lib.oracle_max_threads()
+
+
+def mat4_mul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.empty(16, np.float32)
+    load().lib.oracle_mat4_mul(_p(a), _p(b), _p(out))
+    return out
+
+
+def sphere_transform(m: np.ndarray, s: np.ndarray) -> np.ndarray:
+    m = np.ascontiguousarray(m, np.float32)
+    s = np.ascontiguousarray(s, np.float32)
+    out = np.empty(4, np.float32)
+    load().lib.oracle_sphere_transform(_p(m), _p(s), _p(out))
+    return out
+
+
+def cull(scene, view, threads: int = 0, want_world: bool = False):
+    """Plain pass over a cadr_gb300.scenes.Scene: returns dict with cmds
+    (CMD_DTYPE [N]), counts [S], marginal [ceil(N/32)] and optionally world
+    [N,16] / world_sphere [N,4]."""
+    from cadr_gb300.scenes import CMD_DTYPE
+    L = load().lib
+    n = scene.n
+    S = scene.num_state_sets
+    nl = len(scene.level_local)
+    sizes = np.array(scene.level_sizes + [0], np.uint64)
+    locs = [np.ascontiguousarray(a, np.float32) for a in scene.level_local]
+    pars = [None if p is None else np.ascontiguousarray(p, np.uint32) for p in scene.level_parent]
+    loc_ptrs = (C.c_void_p * max(1, nl))(*[a.ctypes.data for a in locs])
+    par_ptrs = (C.c_void_p * max(1, nl))(*[0 if p is None else p.ctypes.data for p in pars])
+    cmds = np.zeros(n, CMD_DTYPE)
+    counts = np.zeros(S, np.uint32)
+    marginal = np.zeros((n + 31) // 32, np.uint32)
+    world = np.empty((n, 16), np.float32) if want_world else None
+    wsph = np.empty((n, 4), np.float32) if want_world else None
+    view = np.ascontiguousarray(view)
+    rc = L.oracle_cull(nl, _p(sizes), C.cast(loc_ptrs, C.c_void_p), C.cast(par_ptrs, C.c_void_p),
+                       n, _p(scene.local), _p(scene.parent), _p(scene.sphere), _p(scene.geometry),
+                       S, _p(scene.state_set_offsets), scene.num_geometries, scene.num_lods,
+                       _p(scene.lods), _p(view), _p(cmds), _p(counts), _p(marginal), _p(world),
+                       _p(wsph), threads)
+    if rc != 0:
+        raise ValueError("oracle_cull rejected the scene")
+    out = {"cmds": cmds, "counts": counts, "marginal": marginal}
+    if want_world:
+        out["world"], out["world_sphere"] = world, wsph
+    return out
+
+
+def cull_spheres(world_sphere, geometry, offsets, lods, num_lods, view, threads: int = 0):
+    from cadr_gb300.scenes import CMD_DTYPE
+    L = load().lib
+    n = int(world_sphere.shape[0])
+    S = int(offsets.shape[0] - 1)
+    cmds = np.zeros(n, CMD_DTYPE)
+    counts = np.zeros(S, np.uint32)
+    marginal = np.zeros((n + 31) // 32, np.uint32)
+    ws = np.ascontiguousarray(world_sphere, np.float32)
+    rc = L.oracle_cull_spheres(n, _p(ws), _p(geometry), S, _p(offsets), lods.shape[0] // num_lods,
+                               num_lods, _p(lods), _p(np.ascontiguousarray(view)), _p(cmds),
+                               _p(counts), _p(marginal), threads)
+    if rc != 0:
+        raise ValueError("oracle_cull_spheres rejected the input")
+    return {"cmds": cmds, "counts": counts, "marginal": marginal}
+
+
+def process_drawables(image: np.ndarray, image_base: int, handle_level: int, root: int,
+                      drawables: np.ndarray, threads: int = 0):
+    """Tier A over a memory image (uint8 array standing for device memory at
+    image_base).  Returns (indirect uint32 [N,4], pointers uint64 [N,4])."""
+    L = load().lib
+    n = int(drawables.shape[0])
+    ind = np.zeros((n, 4), np.uint32)
+    ptr = np.zeros((n, 4), np.uint64)
+    rc = L.oracle_process_drawables(_p(image), image_base, image.nbytes, handle_level, root,
+                                    _p(np.ascontiguousarray(drawables)), n, _p(ind), _p(ptr),
+                                    threads)
+    if rc != 0:
+        raise ValueError("oracle_process_drawables: a lookup left the memory image")
+    return ind, ptr
+
+
+def valid_cmds(cmds: np.ndarray, counts: np.ndarray, offsets: np.ndarray) -> np.ndarray:
+    """Concatenation of the valid prefix of every StateSet region."""
+    parts = [cmds[int(offsets[s]):int(offsets[s]) + int(counts[s])] for s in range(len(counts))]
+    return np.concatenate(parts) if parts else cmds[:0]

@@ -1,0 +1,359 @@
+/*
+ * cadr_oracle.c - CPU oracle of the drawable-processing pass.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+ * baseline.  See cadr_oracle.h for what each function restates.  Must be
+ * compiled with -ffp-contract=off (oracle/Makefile does).
+ */
+#include "cadr_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int oracle_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+static void set_threads(int threads)
+{
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+}
+
+/* ---------------------------------------------------------------------- */
+/* Tier A: processDrawables.comp:77-113. */
+
+typedef struct image_view {
+    const uint8_t* bytes;
+    uint64_t base;
+    uint64_t size;
+    int bad;
+} image_view;
+
+static uint64_t rd64(image_view* im, uint64_t addr)
+{
+    if (addr < im->base || addr - im->base > im->size - 8 || im->size < 8) {
+        im->bad = 1;
+        return 0;
+    }
+    uint64_t v;
+    memcpy(&v, im->bytes + (addr - im->base), 8);
+    return v;
+}
+
+static uint32_t rd32(image_view* im, uint64_t addr)
+{
+    if (addr < im->base || addr - im->base > im->size - 4 || im->size < 4) {
+        im->bad = 1;
+        return 0;
+    }
+    uint32_t v;
+    memcpy(&v, im->bytes + (addr - im->base), 4);
+    return v;
+}
+
+/* lookupHandle, processDrawables.comp:77-89.  Each index is the 32-bit
+ * truncation the shader applies with uint(...). */
+static uint64_t lookup_handle(image_view* im, uint32_t level, uint64_t root, uint64_t h)
+{
+    if (level == 1) return rd64(im, root + 8ull * (uint32_t)h);
+    if (level == 2) {
+        uint64_t t2 = rd64(im, root + 8ull * (uint32_t)(h >> 11));
+        return rd64(im, t2 + 8ull * ((uint32_t)h & 0x7ffu));
+    }
+    uint64_t t2 = rd64(im, root + 8ull * (uint32_t)(h >> 22));
+    uint64_t t3 = rd64(im, t2 + 8ull * ((uint32_t)(h >> 11) & 0x7ffu));
+    return rd64(im, t3 + 8ull * ((uint32_t)h & 0x7ffu));
+}
+
+int oracle_process_drawables(const uint8_t* image, uint64_t image_base, uint64_t image_size,
+                             uint32_t handle_level, uint64_t handle_table_addr,
+                             const cadr_drawable_gpu_data* drawables, uint64_t n,
+                             cadr_draw_indirect_cmd* indirect, cadr_drawable_pointers* pointers,
+                             int threads)
+{
+    if (handle_level < 1 || handle_level > 3) return -1;
+    int bad = 0;
+    set_threads(threads);
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        image_view im = {image, image_base, image_size, 0};
+        const cadr_drawable_gpu_data* d = &drawables[i];
+        /* main(), processDrawables.comp:95-112 */
+        uint64_t ps = lookup_handle(&im, handle_level, handle_table_addr, d->primitive_set_handle) +
+                      (uint64_t)d->primitive_set_offset;
+        uint64_t ml = lookup_handle(&im, handle_level, handle_table_addr, d->matrix_list_handle);
+        indirect[i].vertex_count = rd32(&im, ps);
+        indirect[i].instance_count = rd32(&im, ml);
+        indirect[i].first_vertex = rd32(&im, ps + 4);
+        indirect[i].first_instance = 0;
+        pointers[i].vertex_data_ptr =
+            lookup_handle(&im, handle_level, handle_table_addr, d->vertex_data_handle);
+        pointers[i].index_data_ptr =
+            lookup_handle(&im, handle_level, handle_table_addr, d->index_data_handle);
+        pointers[i].matrix_list_ptr = ml;
+        pointers[i].drawable_data_ptr =
+            lookup_handle(&im, handle_level, handle_table_addr, d->drawable_data_handle);
+        bad |= im.bad;
+    }
+    return bad ? -1 : 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Tier B arithmetic. */
+
+/* GLM mat4 * mat4 (glm/detail/type_mat4x4.inl operator*):
+ *   Result[c] = SrcA0*B[c][0] + SrcA1*B[c][1] + SrcA2*B[c][2] + SrcA3*B[c][3]
+ * evaluated left to right, one rounding per operation. */
+void oracle_mat4_mul(const float* a, const float* b, float* out)
+{
+    float r[16];
+    for (int c = 0; c < 4; c++) {
+        const float b0 = b[c * 4 + 0], b1 = b[c * 4 + 1], b2 = b[c * 4 + 2], b3 = b[c * 4 + 3];
+        for (int k = 0; k < 4; k++) {
+            float t = a[0 * 4 + k] * b0;
+            t = t + a[1 * 4 + k] * b1;
+            t = t + a[2 * 4 + k] * b2;
+            t = t + a[3 * 4 + k] * b3;
+            r[c * 4 + k] = t;
+        }
+    }
+    memcpy(out, r, sizeof(r));
+}
+
+/* BoundingSphere operator*, src/CadR/BoundingSphere.h:70-86:
+ *   center = mat3(M) * c + vec3(M[3])   (GLM mat3*vec3: m[0][k]*x + m[1][k]*y + m[2][k]*z)
+ *   radius = sqrt(max(max(len2(M[0]), len2(M[1])), len2(M[2]))) * r
+ * with len2(x,y,z) = x*x + y*y + z*z, std::max(a,b) = (a < b) ? b : a, and
+ * the square root and the product by r evaluated in double. */
+void oracle_sphere_transform(const float* m, const float* s, float* out)
+{
+    float c[3];
+    for (int k = 0; k < 3; k++) {
+        float t = m[0 * 4 + k] * s[0];
+        t = t + m[1 * 4 + k] * s[1];
+        t = t + m[2 * 4 + k] * s[2];
+        c[k] = t + m[3 * 4 + k];
+    }
+    float l[3];
+    for (int col = 0; col < 3; col++) {
+        const float x = m[col * 4 + 0], y = m[col * 4 + 1], z = m[col * 4 + 2];
+        float t = x * x;
+        t = t + y * y;
+        l[col] = t + z * z;
+    }
+    float mx = (l[0] < l[1]) ? l[1] : l[0];
+    mx = (mx < l[2]) ? l[2] : mx;
+    out[0] = c[0];
+    out[1] = c[1];
+    out[2] = c[2];
+    /* BoundingSphere.h:85 calls unqualified sqrt() on a float inside
+     * namespace CadR, which resolves to the C library's double sqrt(double):
+     * the reference computes the radius in double and rounds it once to
+     * float on return. */
+    out[3] = (float)(sqrt((double)mx) * (double)s[3]);
+}
+
+int oracle_propagate(const float* parent_world, uint64_t num_parents, const float* local,
+                     const uint32_t* parent, uint64_t n, float* world, int threads)
+{
+    int bad = 0;
+    set_threads(threads);
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        if (!parent) {
+            memcpy(world + 16 * i, local + 16 * i, 64);
+            continue;
+        }
+        uint32_t p = parent[i];
+        if (p >= num_parents) {
+            bad = 1;
+            continue;
+        }
+        oracle_mat4_mul(parent_world + 16ull * p, local + 16 * i, world + 16 * i);
+    }
+    return bad ? -1 : 0;
+}
+
+/* Plane test, marginal band and LOD of one world sphere (project spec):
+ *   dist_p  = ((nx*cx + ny*cy) + nz*cz) + d
+ *   visible = dist_p >= -r for all six planes
+ *   marginal= |dist_p + r| <= 1e-5 * max(1, |d| + r) for some plane
+ *   zc      = perspective ? max(-z_view, near) : 1, z_view = ((vz0*cx+vz1*cy)+vz2*cz)+vz3
+ *   lod     = first k < L-1 with r*lod_scale >= T[k]*zc, else L-1 */
+void oracle_classify(const float* ws, const cadr_view* v, uint32_t num_lods, int* visible,
+                     uint32_t* lod, int* marginal)
+{
+    const float cx = ws[0], cy = ws[1], cz = ws[2], r = ws[3];
+    int vis = 1, mar = 0;
+    for (int p = 0; p < 6; p++) {
+        const float* pl = v->planes[p];
+        float dist = pl[0] * cx;
+        dist = dist + pl[1] * cy;
+        dist = dist + pl[2] * cz;
+        dist = dist + pl[3];
+        if (!(dist >= -r)) vis = 0;
+        float t = dist + r;
+        float tol = 1e-5f * fmaxf(1.0f, fabsf(pl[3]) + r);
+        if (fabsf(t) <= tol) mar = 1;
+    }
+    float zc = 1.0f;
+    if (v->perspective) {
+        float z = v->view_z[0] * cx;
+        z = z + v->view_z[1] * cy;
+        z = z + v->view_z[2] * cz;
+        z = z + v->view_z[3];
+        zc = fmaxf(-z, v->near_z);
+    }
+    const float s = r * v->lod_scale;
+    uint32_t l = num_lods - 1;
+    for (uint32_t k = 0; k + 1 < num_lods; k++) {
+        if (s >= v->lod_threshold[k] * zc) {
+            l = k;
+            break;
+        }
+    }
+    *visible = vis;
+    *lod = l;
+    *marginal = mar;
+}
+
+static int check_offsets(uint64_t n, uint32_t S, const uint32_t* off)
+{
+    if (S == 0 || off[0] != 0 || off[S] != n) return -1;
+    for (uint32_t s = 0; s < S; s++)
+        if (off[s + 1] < off[s]) return -1;
+    return 0;
+}
+
+/* Per-StateSet compaction: visible drawables of StateSet s, in ascending
+ * drawable order, fill cmds[off[s] ...]; counts[s] is their number.  The
+ * regions are the reference's contiguous StateSet regions
+ * (src/CadR/StateSet.cpp:233-261). */
+static int compact(uint64_t n, const uint8_t* vis, const uint8_t* lodv, const uint32_t* geometry,
+                   uint32_t S, const uint32_t* off, uint32_t G, uint32_t L, const cadr_lod* lods,
+                   cadr_draw_indexed_cmd* cmds, uint32_t* counts)
+{
+    (void)n;
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+    for (int64_t s = 0; s < (int64_t)S; s++) {
+        uint32_t k = 0;
+        for (uint32_t i = off[s]; i < off[s + 1]; i++) {
+            if (!vis[i]) continue;
+            uint32_t g = geometry[i];
+            if (g >= G) {
+                bad = 1;
+                continue;
+            }
+            const cadr_lod* e = &lods[(uint64_t)g * L + lodv[i]];
+            cadr_draw_indexed_cmd* c = &cmds[off[s] + k];
+            c->index_count = e->index_count;
+            c->instance_count = 1;
+            c->first_index = e->first_index;
+            c->vertex_offset = e->vertex_offset;
+            c->first_instance = i;
+            k++;
+        }
+        counts[s] = k;
+    }
+    return bad ? -1 : 0;
+}
+
+static void classify_all(uint64_t n, const float* ws, const cadr_view* view, uint32_t L,
+                         uint8_t* vis, uint8_t* lodv, uint32_t* marginal)
+{
+    if (marginal) memset(marginal, 0, ((n + 31) / 32) * 4);
+#pragma omp parallel for schedule(static)
+    for (int64_t w = 0; w < (int64_t)((n + 31) / 32); w++) {
+        uint32_t bits = 0;
+        for (uint64_t i = (uint64_t)w * 32; i < n && i < (uint64_t)w * 32 + 32; i++) {
+            int v, m;
+            uint32_t l;
+            oracle_classify(ws + 4 * i, view, L, &v, &l, &m);
+            vis[i] = (uint8_t)v;
+            lodv[i] = (uint8_t)l;
+            if (m) bits |= 1u << (i & 31);
+        }
+        if (marginal) marginal[w] = bits;
+    }
+}
+
+int oracle_cull_spheres(uint64_t n, const float* world_sphere, const uint32_t* geometry,
+                        uint32_t S, const uint32_t* off, uint32_t G, uint32_t L,
+                        const cadr_lod* lods, const cadr_view* view, cadr_draw_indexed_cmd* cmds,
+                        uint32_t* counts, uint32_t* marginal, int threads)
+{
+    if (L < 1 || L > 4 || check_offsets(n, S, off)) return -1;
+    set_threads(threads);
+    uint8_t* vis = (uint8_t*)malloc(n ? n : 1);
+    uint8_t* lodv = (uint8_t*)malloc(n ? n : 1);
+    if (!vis || !lodv) {
+        free(vis);
+        free(lodv);
+        return -1;
+    }
+    classify_all(n, world_sphere, view, L, vis, lodv, marginal);
+    int rc = compact(n, vis, lodv, geometry, S, off, G, L, lods, cmds, counts);
+    free(vis);
+    free(lodv);
+    return rc;
+}
+
+int oracle_cull(uint32_t num_levels, const uint64_t* level_size, const float* const* level_local,
+                const uint32_t* const* level_parent, uint64_t n, const float* local,
+                const uint32_t* parent, const float* sphere, const uint32_t* geometry, uint32_t S,
+                const uint32_t* off, uint32_t G, uint32_t L, const cadr_lod* lods,
+                const cadr_view* view, cadr_draw_indexed_cmd* cmds, uint32_t* counts,
+                uint32_t* marginal, float* world, float* world_sphere, int threads)
+{
+    if (L < 1 || L > 4 || check_offsets(n, S, off)) return -1;
+    set_threads(threads);
+    int rc = 0;
+    /* Internal levels, top down: level 0's world is its local matrix. */
+    float* prev = NULL;
+    uint64_t prev_n = 0;
+    for (uint32_t l = 0; l < num_levels && rc == 0; l++) {
+        float* w = (float*)malloc(level_size[l] * 64 + 64);
+        if (!w) {
+            rc = -1;
+            break;
+        }
+        if (l == 0)
+            memcpy(w, level_local[0], level_size[0] * 64);
+        else
+            rc = oracle_propagate(prev, prev_n, level_local[l], level_parent[l], level_size[l], w,
+                                  threads);
+        free(prev);
+        prev = w;
+        prev_n = level_size[l];
+    }
+    float* wm = world ? world : (float*)malloc(n * 64 + 64);
+    float* ws = world_sphere ? world_sphere : (float*)malloc(n * 16 + 16);
+    if (!wm || !ws) rc = -1;
+    if (rc == 0)
+        rc = oracle_propagate(prev, prev_n, local, num_levels ? parent : NULL, n, wm, threads);
+    if (rc == 0) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)n; i++)
+            oracle_sphere_transform(wm + 16 * i, sphere + 4 * i, ws + 4 * i);
+        rc = oracle_cull_spheres(n, ws, geometry, S, off, G, L, lods, view, cmds, counts, marginal,
+                                 threads);
+    }
+    free(prev);
+    if (!world) free(wm);
+    if (!world_sphere) free(ws);
+    return rc;
+}

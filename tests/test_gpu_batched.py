@@ -1,0 +1,78 @@
+"""Batched form (one persistent launch over (view, tile) items, CUDA graph
+replay) against the plain pass: identical visible sets and draw buffers."""
+import numpy as np
+import pytest
+
+from cadr_gb300 import lib, scenes
+from helpers import assert_same
+from oracle import bind
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c4_small(ctx):
+    scs = scenes.config4(num_scenes=5, lo=1000, hi=150_000)
+    dss = [lib.DeviceScene(ctx, sc) for sc in scs]
+    for ds in dss:
+        ds.propagate(world_spheres=True)
+    ctx.sync()
+    return scs, dss
+
+
+def _plain(ctx, sc, ds, view):
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    ds.cull(view, out)
+    ctx.sync()
+    return out.fetch()
+
+
+def test_world_spheres_match_oracle(ctx, c4_small):
+    scs, dss = c4_small
+    for sc, ds in zip(scs, dss):
+        ref = bind.cull(sc, sc.views[0], want_world=True)
+        b = ds.buffers()
+        ws = ctx.download(b.world_sphere, np.float32, (sc.n, 4))
+        assert np.array_equal(ws.view(np.uint32), ref["world_sphere"].view(np.uint32))
+        ds.host  # keep alive
+
+
+@pytest.mark.parametrize("tuning", [None, (128, 4, 4), (512, 8, 2), (256, 16, 8)])
+def test_batched_equals_plain(ctx, c4_small, tuning):
+    scs, dss = c4_small
+    items, outs = [], []
+    for sc, ds in zip(scs, dss):
+        ds.buffers  # committed by upload_all
+        for v in sc.views:
+            o = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+            items.append((ds, v, o))
+            outs.append((sc, ds, v, o))
+    arr = lib.batch_views(items)
+    t = lib.Tuning(*tuning, 0) if tuning else None
+    for _ in range(2):  # second call replays the captured graph
+        lib.cull_batched(ctx, arr, t, use_graph=True)
+        ctx.sync()
+        ctx.check_device_error()
+        for sc, ds, v, o in outs:
+            assert_same(o.fetch(), _plain(ctx, sc, ds, v), sc.state_set_offsets)
+
+
+def test_batched_against_oracle_spheres(ctx, c4_small):
+    scs, dss = c4_small
+    sc, ds = scs[-1], dss[-1]
+    items = [(ds, v, lib.CullOutputs(ctx, sc.n, sc.num_state_sets)) for v in sc.views]
+    lib.cull_batched(ctx, lib.batch_views(items), None, use_graph=False)
+    ctx.sync()
+    ref_full = bind.cull(sc, sc.views[0], want_world=True)
+    for (_, v, o) in items:
+        ref = bind.cull_spheres(ref_full["world_sphere"], sc.geometry, sc.state_set_offsets, sc.lods,
+                                sc.num_lods, v)
+        assert_same(o.fetch(), ref, sc.state_set_offsets)
+
+
+def test_autotune_picks_a_supported_tuning(ctx, c4_small):
+    scs, dss = c4_small
+    items = [(ds, v, lib.CullOutputs(ctx, sc.n, sc.num_state_sets)) for sc, ds in zip(scs, dss)
+             for v in sc.views[:2]]
+    t, ms = lib.autotune_batched(ctx, lib.batch_views(items), reps=2)
+    assert t.block_threads in (128, 256, 512) and t.items_per_thread in (4, 8, 16) and ms > 0
