@@ -67,4 +67,6 @@ void destroy_batched_state(cadr_context* ctx);
 cadr_status scene_prepare(cadr_scene* sc, cudaStream_t stream);
 ViewConst to_view_const(const cadr_view& v);
 cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, ViewJob* jobs, uint64_t* total);
+cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream);
+LeafArgs leaf_args(cadr_scene* sc);
 }  // namespace cadr

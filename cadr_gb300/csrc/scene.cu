@@ -60,7 +60,7 @@ static cadr_status after_upload(cadr_scene* sc)
 }
 
 // Propagation of the internal levels 1..L-1 (level 0's world is its local).
-static cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
+cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
 {
     cadr_context* ctx = sc->ctx;
     for (uint32_t l = 1; l < sc->desc.num_levels; l++) {
@@ -75,7 +75,7 @@ static cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
     return CADR_OK;
 }
 
-static LeafArgs leaf_args(cadr_scene* sc)
+LeafArgs leaf_args(cadr_scene* sc)
 {
     const cadr_scene_desc& d = sc->desc;
     LeafArgs a{};

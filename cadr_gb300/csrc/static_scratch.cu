@@ -1,0 +1,109 @@
+// static_scratch.cu - the plain pass with its scratch memory in a statically
+// allocated device array, for callers that cannot allocate device memory.
+//
+// cadr_cull keeps its lookback scratch (the tile counter, the completion
+// counter and one status word per tile of 2,048 drawables) in memory it
+// allocates with cudaMalloc, and grows it, after a device-wide
+// synchronisation, when a scene needs more tiles than it holds.  Some
+// callers cannot let that happen: a renderer whose device memory is owned
+// and budgeted by the host application (every buffer imported or carved
+// out at start-up), or a frame loop that must not stall, since cudaMalloc
+// and cudaFree synchronise the device.  cadr_cull_static_scratch runs the
+// same kernels, with the same results, but takes its scratch from the
+// file-scope array below, which exists on every device that loads this
+// library until the process exits.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "capi_internal.h"
+
+using namespace cadr;
+
+namespace cadr {
+namespace {
+
+// Largest scene the entry point accepts: 16,384 tiles of 2,048 drawables.
+constexpr uint64_t kStaticMaxTiles = 16384;
+constexpr uint64_t kStaticMaxDrawables = kStaticMaxTiles * (uint64_t)kLeafTile;  // 33,554,432
+constexpr size_t kCtlBytes = 256;  // LookbackCtl, padded to keep the tile states 256-byte aligned
+constexpr size_t kStaticScratchBytes = kCtlBytes + kStaticMaxTiles * sizeof(uint64_t);  // 128 KiB + 256 B
+
+// The scratch.  Host code must not take this symbol's address directly: on
+// the host it names a stand-in, not device memory.  The device address comes
+// from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+void* g_scratch_address[kMaxDevices] = {};
+
+// Set-up on the first call per device, with that device current.
+cadr_status static_scratch_address(int device, void** out)
+{
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (device < 0 || device >= kMaxDevices)
+        return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: device %d out of range", device);
+    if (!g_scratch_address[device]) {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: set device");
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: scratch address");
+        g_scratch_address[device] = p;
+    }
+    *out = g_scratch_address[device];
+    return CADR_OK;
+}
+
+}  // namespace
+}  // namespace cadr
+
+extern "C" {
+
+CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* view, cadr_draw_indexed_cmd* cmds,
+                                              uint32_t* counts, uint32_t* marginal, cadr_stream stream)
+{
+    if (!sc || !view || !counts || (!cmds && sc->desc.num_drawables))
+        return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: null argument");
+    if (!sc->committed)
+        return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: commit the scene (cadr_scene_commit) first");
+    if (sc->desc.num_drawables > kStaticMaxDrawables)
+        return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: %llu drawables exceed the maximum of %llu",
+                    (unsigned long long)sc->desc.num_drawables, (unsigned long long)kStaticMaxDrawables);
+    cadr_context* ctx = sc->ctx;
+    void* base = nullptr;
+    cadr_status st = static_scratch_address(ctx->device, &base);
+    if (st != CADR_OK) return st;
+    cudaStream_t s = pick_stream(ctx, stream);
+    st = scene_prepare(sc, s);
+    if (st != CADR_OK) return st;
+    cudaError_t e;
+    if (sc->desc.num_drawables == 0) {
+        e = cudaMemsetAsync(counts, 0, (size_t)sc->desc.num_state_sets * 4, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: clear counts");
+        return CADR_OK;
+    }
+    const uint64_t tiles = (sc->desc.num_drawables + kLeafTile - 1) / kLeafTile;
+    Scratch scratch;
+    scratch.ctl = static_cast<LookbackCtl*>(base);
+    scratch.tile_state = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(base) + kCtlBytes);
+    scratch.capacity = kStaticMaxTiles;
+    // The array keeps the previous call's contents: zero the control block
+    // and this pass's tile states (epoch 0, nothing published) first.
+    e = cudaMemsetAsync(base, 0, kCtlBytes + tiles * sizeof(uint64_t), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: clear scratch");
+    st = propagate_levels(sc, s);
+    if (st != CADR_OK) return st;
+    LeafArgs a = leaf_args(sc);
+    a.cmds = reinterpret_cast<uint32_t*>(cmds);
+    a.counts = counts;
+    a.marginal = marginal;
+    a.view = to_view_const(*view);
+    e = launch_leaf_cull(a, scratch, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: launch");
+    ctx->launches++;
+    return CADR_OK;
+}
+
+}  // extern "C"

@@ -253,6 +253,26 @@ CADR_API cadr_status cadr_cull(cadr_scene* scene, const cadr_view* view,
                                cadr_draw_indexed_cmd* cmds, uint32_t* counts,
                                uint32_t* marginal, cadr_stream stream);
 
+/* The plain pass without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory while they run: a renderer whose device memory is owned and
+ * budgeted by the host application, or a frame loop that cannot afford the
+ * device-wide synchronisation of cudaMalloc/cudaFree, which cadr_cull may
+ * perform when a scene needs more lookback scratch than it holds.  Same
+ * kernels and bit-identical results as cadr_cull; the caller still passes
+ * the outputs.  The scratch is a static device array of 128 KiB + 256 B
+ * (held by every GPU that loads the library until exit), which limits scenes
+ * to 33,554,432 drawables; larger ones are rejected with
+ * CADR_ERR_INVALID_ARG, as are scenes not committed yet.  The first call on
+ * a device looks up the array's device address (set-up): make that first
+ * call before any stream capture.  Every call shares the one array, which
+ * keeps the last call's contents (each call clears what must start at
+ * zero), so calls whose work overlaps on the GPU race: keep them on one
+ * stream or otherwise ordered. */
+CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* scene, const cadr_view* view,
+                                              cadr_draw_indexed_cmd* cmds, uint32_t* counts,
+                                              uint32_t* marginal, cadr_stream stream);
+
 /* Batched form: many (scene, view) pairs culled by one persistent launch over
  * (view, tile) work items, replayed from a captured CUDA graph when the
  * same batch shape repeats.  Scenes must have been propagated with
