@@ -69,7 +69,30 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_facade(force=force)
     return LIB
+
+
+FACADE_DIR = os.path.join(HERE, "facade")
+FACADE_LIB = os.path.join(OUT_DIR, "libcadr.so")
+
+
+def build_facade(force: bool = False) -> str:
+    """The C++ facade (include/CadR/*.h) over the C ABI: libcadr.so, which
+    links libcadr_cuda.so from the same directory."""
+    srcs = sorted(os.path.join(FACADE_DIR, f) for f in os.listdir(FACADE_DIR) if f.endswith(".cpp"))
+    inc = os.path.join(ROOT, "include")
+    deps = srcs + [os.path.join(inc, "cadr_cuda.h")] + [
+        os.path.join(inc, "CadR", f) for f in os.listdir(os.path.join(inc, "CadR"))]
+    if not force and not _stale(FACADE_LIB, deps + [LIB]):
+        return FACADE_LIB
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", "-I", inc, *srcs, "-o", FACADE_LIB,
+           "-L", OUT_DIR, "-lcadr_cuda", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"facade build failed:\n{r.stdout}\n{r.stderr}")
+    return FACADE_LIB
 
 
 if __name__ == "__main__":

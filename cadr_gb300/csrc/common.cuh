@@ -101,6 +101,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
                  : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// Retires an mbarrier before its shared memory is given back.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar)
+{
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
@@ -129,6 +134,24 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
 }
+// Bulk (TMA) copy shared -> global, tracked by the issuing thread's bulk
+// groups.  Requires 16-byte aligned dst/src and bytes % 16 == 0.
+__device__ __forceinline__ void bulk_copy_s2g(void* dst, const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+                 "r"(smem_addr(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Wait until all committed bulk groups of this thread have finished reading
+// their shared-memory source (the buffer may be overwritten afterwards).
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Wait until all committed bulk groups of this thread are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Orders this thread's generic-proxy shared-memory writes before later
+// async-proxy (TMA) accesses of that memory.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // Bounded wait on phase `parity`; returns false (after limit_ns) when the
 // barrier never completed.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)

@@ -28,7 +28,7 @@ __device__ __forceinline__ void load_mat(const float4* __restrict__ p, float4& c
 using LeafTile = Tile<kLeafThreads, kLeafIpt>;
 
 template <bool kCull>
-__global__ void __launch_bounds__(kLeafThreads, 2) leaf_kernel(const LeafArgs a, const Scratch s)
+__global__ void __launch_bounds__(kLeafThreads, 4) leaf_kernel(const LeafArgs a, const Scratch s)
 {
     __shared__ LeafTile::Smem sm;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;

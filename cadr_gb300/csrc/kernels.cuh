@@ -77,6 +77,11 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 // select LOD, compact per StateSet.
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream);
 
+// The same pass as a persistent double-buffered TMA kernel (1 CTA per SM,
+// tiles of leaf_tma_tile() drawables); used by cadr_cull.
+cudaError_t launch_leaf_cull_tma(const LeafArgs& a, Scratch& s, int num_sms, int device, cudaStream_t stream);
+uint32_t leaf_tma_tile();
+
 // Batched sphere cull: one persistent launch over all (view, tile) items.
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items,
                                 Scratch& s, uint32_t* error, uint64_t spin_limit_ns,

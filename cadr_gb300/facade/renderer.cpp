@@ -1,0 +1,215 @@
+// renderer.cpp - Geometry, MatrixList, Drawable, StateSet and Renderer of
+// the C++ facade (src/CadR/Drawable.cpp, StateSet.cpp, Renderer.cpp).
+#include <CadR/Renderer.h>
+
+#include <algorithm>
+#include <cstring>
+
+namespace CadR {
+
+Geometry::Geometry(Renderer& r)
+    : _vertices(r.dataStorage()), _indices(r.dataStorage()), _primitiveSets(r.dataStorage())
+{
+}
+
+MatrixList::MatrixList(Renderer& r) : _list(r.dataStorage()) {}
+
+// Header {numMatrices, capacity, 7 x uint64 0} then the matrices
+// (MatrixList.h:54-58).
+void MatrixList::setMatrices(const Mat4* m, size_t n)
+{
+    StagingData s = _list.alloc(64 + 64 * n);
+    uint8_t* p = s.data<uint8_t>();
+    std::memset(p, 0, 64);
+    const uint32_t n32 = uint32_t(n);
+    std::memcpy(p, &n32, 4);
+    std::memcpy(p + 4, &n32, 4);
+    if (n) std::memcpy(p + 64, m, 64 * n);
+}
+
+// ---------------------------------------------------------------------------
+// Drawable (Drawable.cpp:35-78).
+
+Drawable::Drawable(Geometry& g, uint32_t off, MatrixList& ml, StateSet& ss)
+{
+    ss.append(*this, DrawableGpuData{g.vertexDataAllocation().handle(), g.indexDataAllocation().handle(), ml.handle(),
+                                     0, g.primitiveSetDataAllocation().handle(), off, 0});
+}
+
+Drawable::Drawable(Geometry& g, uint32_t off, MatrixList& ml, DataAllocation& dd, StateSet& ss)
+{
+    ss.append(*this, DrawableGpuData{g.vertexDataAllocation().handle(), g.indexDataAllocation().handle(), ml.handle(),
+                                     dd.handle(), g.primitiveSetDataAllocation().handle(), off, 0});
+}
+
+Drawable::Drawable(Drawable&& o) noexcept : _stateSet(o._stateSet), _index(o._index)
+{
+    if (_index != ~0u) _stateSet->_drawables[_index] = this;
+    o._index = ~0u;
+}
+
+Drawable::~Drawable() { destroy(); }
+
+void Drawable::destroy() noexcept
+{
+    if (_index != ~0u) _stateSet->remove(*this);
+}
+
+// ---------------------------------------------------------------------------
+// StateSet (StateSet.cpp:20-47,180-268).
+
+StateSet::~StateSet()
+{
+    for (Drawable* d : _drawables) d->_index = ~0u;
+}
+
+void StateSet::removeChild(StateSet& child)
+{
+    auto it = std::find(childList.begin(), childList.end(), &child);
+    if (it != childList.end()) childList.erase(it);
+}
+
+void StateSet::append(Drawable& d, const DrawableGpuData& g)
+{
+    d._stateSet = this;
+    d._index = uint32_t(_records.size());
+    _records.push_back(g);
+    _drawables.push_back(&d);
+}
+
+// O(1) removal: the last record takes the removed one's place.
+void StateSet::remove(Drawable& d) noexcept
+{
+    const uint32_t i = d._index;
+    const size_t last = _records.size() - 1;
+    if (i != last) {
+        _records[i] = _records[last];
+        Drawable* moved = _drawables[last];
+        _drawables[i] = moved;
+        moved->_index = i;
+    }
+    _records.pop_back();
+    _drawables.pop_back();
+    d._index = ~0u;
+}
+
+size_t StateSet::prepareRecording()
+{
+    _skipRecording = !_forceRecording;
+    size_t n = _records.size();
+    for (StateSet* c : childList) {
+        n += c->prepareRecording();
+        _skipRecording = _skipRecording && c->_skipRecording;
+    }
+    _skipRecording = _skipRecording && n == 0;
+    return n;
+}
+
+void StateSet::recordToCommandBuffer(std::vector<DrawCall>& out, size_t& counter)
+{
+    if (_skipRecording) return;
+    const size_t n = _records.size();
+    if (n > 0) {
+        std::memcpy(_renderer->drawableStagingData() + counter, _records.data(), n * sizeof(DrawableGpuData));
+        out.push_back(DrawCall{this, counter, uint32_t(n),
+                               _renderer->drawablePointersBufferAddress() + counter * Renderer::drawablePointersRecordSize,
+                               counter * sizeof(cadr_draw_indirect_cmd)});
+        counter += n;
+    }
+    for (StateSet* c : childList) c->recordToCommandBuffer(out, counter);
+}
+
+// ---------------------------------------------------------------------------
+// Renderer.
+
+Renderer::Renderer(int device)
+{
+    check(cadr_context_create(device, &_ownContext), "Renderer: context");
+    _ownBackend = std::make_unique<CudaMemoryBackend>(_ownContext);
+    _backend = _ownBackend.get();
+    _storage = std::make_unique<DataStorage>(*_backend);
+}
+
+Renderer::Renderer(MemoryBackend& backend) : _backend(&backend)
+{
+    _storage = std::make_unique<DataStorage>(*_backend);
+}
+
+Renderer::~Renderer()
+{
+    if (_ownContext) cadr_context_synchronize(_ownContext);
+    if (_drawables) _backend->freeBlock(_drawables);
+    if (_indirect) _backend->freeBlock(_indirect);
+    if (_pointers) _backend->freeBlock(_pointers);
+    _storage.reset();
+    _ownBackend.reset();
+    if (_ownContext) cadr_context_destroy(_ownContext);
+}
+
+size_t Renderer::beginFrame()
+{
+    _frame++;
+    _storage->setFrameNumber(_frame);
+    return _frame;
+}
+
+void Renderer::endFrame() {}
+
+// Buffer growth of Renderer::prepareSceneRendering (Renderer.cpp:461-592):
+// 20% extra, at least 128 drawables.
+void Renderer::growBuffers(size_t n)
+{
+    if (_capacity >= n) return;
+    size_t cap = size_t(float(n) * 1.2f);
+    if (cap < 128) cap = 128;
+    if (_ownContext) cadr_context_synchronize(_ownContext);
+    if (_drawables) _backend->freeBlock(_drawables);
+    if (_indirect) _backend->freeBlock(_indirect);
+    if (_pointers) _backend->freeBlock(_pointers);
+    _drawables = _backend->allocBlock(cap * sizeof(DrawableGpuData));
+    _indirect = _backend->allocBlock(cap * sizeof(cadr_draw_indirect_cmd));
+    _pointers = _backend->allocBlock(cap * drawablePointersRecordSize);
+    if (!_drawables || !_indirect || !_pointers) throw OutOfResources("Renderer: cannot allocate drawable buffers");
+    _staging.assign(cap, DrawableGpuData{});
+    _capacity = cap;
+}
+
+size_t Renderer::prepareSceneRendering(StateSet& root)
+{
+    const size_t n = root.prepareRecording();
+    growBuffers(n);
+    return n;
+}
+
+void Renderer::recordSceneRendering(StateSet& root, std::vector<DrawCall>& out)
+{
+    size_t counter = 0;
+    root.recordToCommandBuffer(out, counter);
+}
+
+size_t Renderer::executeCopyOperations() { return _storage->uploadPending(); }
+
+void Renderer::recordDrawableProcessing(size_t n, cadr_stream stream)
+{
+    if (n == 0) return;
+    cadr_context* ctx = _backend->context();
+    if (!ctx) throw LogicError("Renderer::recordDrawableProcessing(): this renderer has no CUDA context");
+    if (n > _capacity) throw LogicError("Renderer::recordDrawableProcessing(): call prepareSceneRendering() first");
+    check(cadr_upload(ctx, reinterpret_cast<void*>(_drawables), _staging.data(), n * sizeof(DrawableGpuData), stream),
+          "Renderer: drawable upload");
+    check(cadr_process_drawables(ctx, _storage->handleLevel(), reinterpret_cast<const void*>(_storage->handleTableDeviceAddress()),
+                                 reinterpret_cast<const cadr_drawable_gpu_data*>(_drawables), n,
+                                 reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
+                                 reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
+          "Renderer: processDrawables");
+}
+
+void Renderer::processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream)
+{
+    const size_t n = prepareSceneRendering(root);
+    recordSceneRendering(root, out);
+    executeCopyOperations();
+    recordDrawableProcessing(n, stream);
+}
+
+}  // namespace CadR

@@ -1,0 +1,191 @@
+// CadR/Renderer.h - the scene objects and the frame driver of the C++
+// facade: Geometry, PrimitiveSet, MatrixList, Drawable, StateSet, Renderer,
+// with the reference's names, data layouts and recording order.
+//
+//   Geometry     three DataAllocations: vertices, indices, PrimitiveSets
+//                (src/CadR/Geometry.h:37-39)
+//   MatrixList   64-byte header {numMatrices, capacity, 0...} + mat4[n]
+//                (src/CadR/MatrixList.h:54-59)
+//   Drawable     one DrawableGpuData record in its StateSet's list
+//                (src/CadR/Drawable.h:32-43, Drawable.cpp:35-78)
+//   StateSet     per-StateSet record list with O(1) swap-remove, child list,
+//                prepareRecording / recordToCommandBuffer in depth-first
+//                order (src/CadR/StateSet.cpp:20-47,180-268)
+//   Renderer     buffer growth x1.2 (min 128), drawable processing through
+//                cadr_process_drawables, uploads, frame timing
+//                (src/CadR/Renderer.cpp:446-720,946-999)
+//
+// Difference from the reference: there is no deferred command buffer, so
+// recordDrawableProcessing() runs the pass when called and must come after
+// recordSceneRendering() has packed the records (processDrawables() does
+// the three steps in that order).  Matrices are column-major float[16].
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "DataStorage.h"
+
+namespace CadR {
+
+using Mat4 = std::array<float, 16>;
+
+struct PrimitiveSet {
+    uint32_t indexCount;
+    uint32_t startIndex;
+};
+static_assert(sizeof(PrimitiveSet) == 8, "PrimitiveSet layout");
+
+struct DrawableGpuData {
+    uint64_t vertexDataHandle;
+    uint64_t indexDataHandle;
+    uint64_t matrixListHandle;
+    uint64_t drawableDataHandle;
+    uint64_t primitiveSetHandle;
+    uint32_t primitiveSetOffset;
+    uint32_t padding;
+};
+static_assert(sizeof(DrawableGpuData) == 48, "DrawableGpuData must be 48 bytes (Drawable.cpp:13)");
+static_assert(sizeof(DrawableGpuData) == sizeof(cadr_drawable_gpu_data), "C ABI record");
+
+class Renderer;
+class StateSet;
+
+class Geometry {
+public:
+    explicit Geometry(Renderer& r);
+    void uploadVertexData(const void* p, size_t n) { _vertices.upload(p, n); }
+    void uploadIndexData(const void* p, size_t n) { _indices.upload(p, n); }
+    void uploadPrimitiveSetData(const void* p, size_t n) { _primitiveSets.upload(p, n); }
+    DataAllocation& vertexDataAllocation() { return _vertices; }
+    DataAllocation& indexDataAllocation() { return _indices; }
+    DataAllocation& primitiveSetDataAllocation() { return _primitiveSets; }
+
+private:
+    DataAllocation _vertices, _indices, _primitiveSets;
+};
+
+class MatrixList {
+public:
+    explicit MatrixList(Renderer& r);
+    void setMatrices(const Mat4& m) { setMatrices(&m, 1); }
+    void setMatrices(const std::vector<Mat4>& m) { setMatrices(m.data(), m.size()); }
+    void setMatrices(const Mat4* m, size_t n);
+    uint64_t handle() const { return _list.handle(); }
+    uint64_t deviceAddress() const { return _list.deviceAddress(); }
+
+private:
+    DataAllocation _list;
+};
+
+class Drawable {
+public:
+    Drawable() = default;
+    Drawable(Geometry& g, uint32_t primitiveSetOffset, MatrixList& ml, StateSet& ss);
+    Drawable(Geometry& g, uint32_t primitiveSetOffset, MatrixList& ml, DataAllocation& drawableData, StateSet& ss);
+    Drawable(Drawable&& other) noexcept;
+    Drawable(const Drawable&) = delete;
+    Drawable& operator=(const Drawable&) = delete;
+    ~Drawable();
+    void destroy() noexcept;
+    bool isValid() const { return _index != ~0u; }
+    StateSet& stateSet() const { return *_stateSet; }
+
+private:
+    StateSet* _stateSet = nullptr;
+    uint32_t _index = ~0u;
+    friend class StateSet;
+};
+
+// What StateSet::recordToCommandBuffer records for one StateSet with
+// drawables: cmdPushConstants(offset 8, pointersBase + first*32) and
+// cmdDrawIndirect(indirectBuffer, first*16, count, 16) (StateSet.cpp:240-258).
+struct DrawCall {
+    const StateSet* stateSet;
+    uint64_t first;              // drawableCounter
+    uint32_t count;
+    uint64_t drawablePointers;   // device address of the region's DrawablePointers
+    uint64_t indirectOffset;     // byte offset into the indirect buffer
+};
+
+class StateSet {
+public:
+    explicit StateSet(Renderer& r) : _renderer(&r) {}
+    ~StateSet();
+    StateSet(const StateSet&) = delete;
+    StateSet& operator=(const StateSet&) = delete;
+
+    void appendChild(StateSet& child) { childList.push_back(&child); }
+    void removeChild(StateSet& child);
+    size_t getNumDrawables() const { return _records.size(); }
+    const std::vector<DrawableGpuData>& drawableDataList() const { return _records; }
+    void setForceRecording(bool v) { _forceRecording = v; }
+
+    size_t prepareRecording();
+    void recordToCommandBuffer(std::vector<DrawCall>& out, size_t& drawableCounter);
+
+    std::vector<StateSet*> childList;
+
+private:
+    void append(Drawable& d, const DrawableGpuData& g);
+    void remove(Drawable& d) noexcept;
+    Renderer* _renderer;
+    bool _skipRecording = true;
+    bool _forceRecording = false;
+    std::vector<DrawableGpuData> _records;
+    std::vector<Drawable*> _drawables;
+    friend class Drawable;
+};
+
+// CadR::FrameInfo counterpart: GPU times of the last processed frame.
+struct FrameInfo {
+    size_t frameNumber = ~size_t(0);
+    float uploadMs = 0;       // executeCopyOperations + record copy
+    float processingMs = 0;   // the drawable-processing kernel
+};
+
+class Renderer {
+public:
+    // Renderer on CUDA device `device` (its own cadr_context).
+    explicit Renderer(int device = 0);
+    // Renderer over a caller-provided backend; without a context only the
+    // host side (allocation, handles, recording) is available.
+    explicit Renderer(MemoryBackend& backend);
+    ~Renderer();
+    Renderer(const Renderer&) = delete;
+    Renderer& operator=(const Renderer&) = delete;
+
+    DataStorage& dataStorage() { return *_storage; }
+    cadr_context* context() const { return _backend->context(); }
+    size_t frameNumber() const { return _frame; }
+
+    size_t beginFrame();
+    size_t prepareSceneRendering(StateSet& root);
+    void recordSceneRendering(StateSet& root, std::vector<DrawCall>& out);
+    void recordDrawableProcessing(size_t numDrawables, cadr_stream stream = nullptr);
+    void processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream = nullptr);
+    void endFrame();
+    size_t executeCopyOperations();
+
+    DrawableGpuData* drawableStagingData() const { return _staging.data(); }
+    size_t drawableBufferSize() const { return _capacity * sizeof(DrawableGpuData); }
+    uint64_t drawableBufferAddress() const { return _drawables; }
+    uint64_t drawIndirectBufferAddress() const { return _indirect; }
+    uint64_t drawablePointersBufferAddress() const { return _pointers; }
+    static constexpr uint32_t drawablePointersRecordSize = 32;
+
+private:
+    void growBuffers(size_t numDrawables);
+    std::unique_ptr<MemoryBackend> _ownBackend;
+    MemoryBackend* _backend;
+    cadr_context* _ownContext = nullptr;
+    std::unique_ptr<DataStorage> _storage;
+    size_t _frame = ~size_t(0);
+    size_t _capacity = 0;
+    uint64_t _drawables = 0, _indirect = 0, _pointers = 0;
+    mutable std::vector<DrawableGpuData> _staging;
+};
+
+}  // namespace CadR

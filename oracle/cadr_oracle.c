@@ -36,31 +36,36 @@ static void set_threads(int threads)
 /* Tier A: processDrawables.comp:77-113. */
 
 typedef struct image_view {
-    const uint8_t* bytes;
-    uint64_t base;
-    uint64_t size;
+    const oracle_region* r;
+    uint32_t n;
     int bad;
 } image_view;
 
+/* Host bytes of [addr, addr + len) when one region holds all of them. */
+static const uint8_t* locate(image_view* im, uint64_t addr, uint64_t len)
+{
+    for (uint32_t k = 0; k < im->n; k++) {
+        const oracle_region* g = &im->r[k];
+        if (g->size >= len && addr >= g->base && addr - g->base <= g->size - len)
+            return g->bytes + (addr - g->base);
+    }
+    im->bad = 1;
+    return NULL;
+}
+
 static uint64_t rd64(image_view* im, uint64_t addr)
 {
-    if (addr < im->base || addr - im->base > im->size - 8 || im->size < 8) {
-        im->bad = 1;
-        return 0;
-    }
-    uint64_t v;
-    memcpy(&v, im->bytes + (addr - im->base), 8);
+    const uint8_t* p = locate(im, addr, 8);
+    uint64_t v = 0;
+    if (p) memcpy(&v, p, 8);
     return v;
 }
 
 static uint32_t rd32(image_view* im, uint64_t addr)
 {
-    if (addr < im->base || addr - im->base > im->size - 4 || im->size < 4) {
-        im->bad = 1;
-        return 0;
-    }
-    uint32_t v;
-    memcpy(&v, im->bytes + (addr - im->base), 4);
+    const uint8_t* p = locate(im, addr, 4);
+    uint32_t v = 0;
+    if (p) memcpy(&v, p, 4);
     return v;
 }
 
@@ -84,12 +89,23 @@ int oracle_process_drawables(const uint8_t* image, uint64_t image_base, uint64_t
                              cadr_draw_indirect_cmd* indirect, cadr_drawable_pointers* pointers,
                              int threads)
 {
+    const oracle_region r = {image, image_base, image_size};
+    return oracle_process_drawables_regions(&r, 1, handle_level, handle_table_addr, drawables, n,
+                                            indirect, pointers, threads);
+}
+
+int oracle_process_drawables_regions(const oracle_region* regions, uint32_t num_regions,
+                                     uint32_t handle_level, uint64_t handle_table_addr,
+                                     const cadr_drawable_gpu_data* drawables, uint64_t n,
+                                     cadr_draw_indirect_cmd* indirect,
+                                     cadr_drawable_pointers* pointers, int threads)
+{
     if (handle_level < 1 || handle_level > 3) return -1;
     int bad = 0;
     set_threads(threads);
 #pragma omp parallel for schedule(static) reduction(| : bad)
     for (int64_t i = 0; i < (int64_t)n; i++) {
-        image_view im = {image, image_base, image_size, 0};
+        image_view im = {regions, num_regions, 0};
         const cadr_drawable_gpu_data* d = &drawables[i];
         /* main(), processDrawables.comp:95-112 */
         uint64_t ps = lookup_handle(&im, handle_level, handle_table_addr, d->primitive_set_handle) +

@@ -37,6 +37,19 @@ int oracle_process_drawables(const uint8_t* image, uint64_t image_base, uint64_t
                              cadr_draw_indirect_cmd* indirect, cadr_drawable_pointers* pointers,
                              int threads);
 
+/* The same over several regions of device memory (e.g. the DataMemory
+ * blocks of a DataStorage, downloaded to the host). */
+typedef struct oracle_region {
+    const uint8_t* bytes;
+    uint64_t base;
+    uint64_t size;
+} oracle_region;
+int oracle_process_drawables_regions(const oracle_region* regions, uint32_t num_regions,
+                                     uint32_t handle_level, uint64_t handle_table_addr,
+                                     const cadr_drawable_gpu_data* drawables, uint64_t n,
+                                     cadr_draw_indirect_cmd* indirect,
+                                     cadr_drawable_pointers* pointers, int threads);
+
 /* GLM-order 4x4 product out = a * b (column-major float[16]). */
 void oracle_mat4_mul(const float* a, const float* b, float* out);
 /* BoundingSphere operator*: out = m * (cx, cy, cz, r). */
