@@ -34,6 +34,10 @@ struct BatchedState {
 
 namespace {
 
+// StateSet offsets of the current view's scene are staged in shared memory
+// up to this many entries (8 KiB).
+constexpr uint32_t kBatchedOffsetCap = 2048;
+
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
                                                          uint32_t total_items, const Scratch s, uint32_t* error,
@@ -45,8 +49,10 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
     __shared__ uint32_t s_job;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    extern __shared__ uint32_t s_offsets[];
     if (t == 0) sm.info[1] = load_relaxed_u32(&s.ctl->epoch);
     uint32_t cur_job = 0xffffffffu;
+    const uint32_t* off = nullptr;
     for (;;) {
         if (t == 0) {
             const uint32_t item = atomicAdd(&s.ctl->tile_counter, 1u);
@@ -70,6 +76,8 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
             uint32_t* dst = reinterpret_cast<uint32_t*>(&job);
             for (int k = t; k < (int)(sizeof(ViewJob) / 4); k += THREADS) dst[k] = __ldg(src + k);
             __syncthreads();
+            // published by the __syncthreads() that follows the item loop
+            off = stage_offsets(s_offsets, kBatchedOffsetCap, job.offsets, job.num_state_sets);
         }
         const uint32_t b = (item - job.first_item) * (uint32_t)T::SIZE;
         uint32_t vis_bits = 0, lod_bits = 0;
@@ -96,9 +104,9 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
             lod_bits |= lod << (2 * j);
         }
         __syncthreads();
-        T::scan(sm, job.offsets, job.num_state_sets, b, job.n);
-        T::lookback(sm, s.tile_state, item, job.first_item, job.offsets, b, limit_ns, 0u, error);
-        T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, job.offsets, job.num_state_sets,
+        T::scan(sm, off, job.num_state_sets, b, job.n);
+        T::lookback(sm, s.tile_state, item, job.first_item, off, b, limit_ns, 0u, error);
+        T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, off, job.num_state_sets,
                  job.lods, job.num_geometries, job.num_lods, job.cmds, job.counts, error);
         __syncthreads();
     }
@@ -141,7 +149,8 @@ cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32
 {
     KernelFn k = pick_kernel(block_threads, items_per_thread);
     if (!k) return cudaErrorInvalidValue;
-    k<<<grid, block_threads, 0, stream>>>(d_jobs, num_jobs, total_items, s, error, spin_limit_ns);
+    k<<<grid, block_threads, kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s, error,
+                                                                          spin_limit_ns);
     return cudaGetLastError();
 }
 

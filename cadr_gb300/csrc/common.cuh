@@ -152,6 +152,14 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 // async-proxy (TMA) accesses of that memory.
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Bulk (TMA) prefetch of [src, src + bytes) into L2; 16-byte aligned
+// address, bytes % 16 == 0.  Brings a whole tile's stream on its way with
+// one instruction and no registers.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Bounded wait on phase `parity`; returns false (after limit_ns) when the
 // barrier never completed.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
@@ -241,18 +249,29 @@ __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, ui
 }
 
 // First index s in [lo, hi) with offsets[s] > key, minus one: the region
-// that contains position `key` (regions may be empty).
-__device__ __forceinline__ uint32_t region_of(const uint32_t* __restrict__ offsets, uint32_t lo,
-                                              uint32_t hi, uint32_t key)
+// that contains position `key` (regions may be empty).  `offsets` may point
+// to global or (staged) shared memory.
+__device__ __forceinline__ uint32_t region_of(const uint32_t* offsets, uint32_t lo, uint32_t hi, uint32_t key)
 {
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(offsets + mid) <= key)
+        if (offsets[mid] <= key)
             lo = mid + 1;
         else
             hi = mid;
     }
     return lo - 1;
+}
+
+// Stages the S+1 StateSet offsets into shared memory when they fit `cap`
+// entries (all threads of the CTA call it; the caller's next
+// __syncthreads() publishes them) and returns the array to search.
+__device__ __forceinline__ const uint32_t* stage_offsets(uint32_t* smem, uint32_t cap, const uint32_t* offsets,
+                                                         uint32_t S)
+{
+    if (S + 1 > cap) return offsets;
+    for (uint32_t k = threadIdx.x; k <= S; k += blockDim.x) smem[k] = __ldg(offsets + k);
+    return smem;
 }
 
 }  // namespace cadr

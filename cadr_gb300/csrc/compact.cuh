@@ -142,7 +142,7 @@ struct Tile {
         if (warp == 0) {
             const uint32_t total = sm.info[3];
             const uint32_t epoch = sm.info[1];
-            const uint32_t last_start = __ldg(offsets + sm.info[5]);
+            const uint32_t last_start = offsets[sm.info[5]];
             const uint32_t head = last_start >= b ? 1u : 0u;
             const uint32_t val = head ? total - excl(sm, last_start - b) : total;
             uint32_t carry = 0;
@@ -176,13 +176,13 @@ struct Tile {
     {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
-        const uint32_t start_f = __ldg(offsets + rf);
+        const uint32_t start_f = offsets[rf];
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
             if (!((vis_bits >> j) & 1u)) continue;
             const uint32_t i = b + (uint32_t)(j * THREADS + t);
             const uint32_t r = (rf == rl) ? rf : region_of(offsets, rf, rl + 1, i);
-            const uint32_t start = (r == rf) ? start_f : __ldg(offsets + r);
+            const uint32_t start = (r == rf) ? start_f : offsets[r];
             const uint32_t ei = excl(sm, i - b);
             const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
             uint32_t g = geo[j];
@@ -200,7 +200,7 @@ struct Tile {
         }
         const uint32_t e_tile = min(b + (uint32_t)SIZE, n);
         for (uint32_t k = rf + (uint32_t)t; k <= rl; k += THREADS) {
-            const uint32_t sk = __ldg(offsets + k), ek = __ldg(offsets + k + 1);
+            const uint32_t sk = offsets[k], ek = offsets[k + 1];
             if (ek > sk && ek > b && ek <= e_tile) {
                 const uint32_t ee = excl(sm, ek - b);
                 counts[k] = (sk >= b) ? ee - excl(sm, sk - b) : carry + ee;
@@ -208,7 +208,7 @@ struct Tile {
         }
         if (first_tile)
             for (uint32_t k = (uint32_t)t; k < S; k += THREADS)
-                if (__ldg(offsets + k) == __ldg(offsets + k + 1)) counts[k] = 0u;
+                if (offsets[k] == offsets[k + 1]) counts[k] = 0u;
     }
 };
 

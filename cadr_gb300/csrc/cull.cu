@@ -50,6 +50,8 @@ __global__ void __launch_bounds__(kLeafThreads, 4) leaf_kernel(const LeafArgs a,
         return;
     }
     const uint32_t b = tile * (uint32_t)kLeafTile;
+    extern __shared__ uint32_t s_offsets[];
+    const uint32_t* off = kCull ? stage_offsets(s_offsets, a.off_cap, a.offsets, a.num_state_sets) : a.offsets;
 
     uint32_t vis_bits = 0, lod_bits = 0;
     uint32_t geo[kLeafIpt];
@@ -105,9 +107,9 @@ __global__ void __launch_bounds__(kLeafThreads, 4) leaf_kernel(const LeafArgs a,
     }
     if (!kCull) return;
     __syncthreads();
-    LeafTile::scan(sm, a.offsets, a.num_state_sets, b, a.n);
-    LeafTile::lookback(sm, s.tile_state, tile, 0, a.offsets, b, a.spin_limit_ns, a.fault, a.error);
-    LeafTile::write(sm, vis_bits, lod_bits, geo, b, a.n, tile == 0, a.offsets, a.num_state_sets, a.lods,
+    LeafTile::scan(sm, off, a.num_state_sets, b, a.n);
+    LeafTile::lookback(sm, s.tile_state, tile, 0, off, b, a.spin_limit_ns, a.fault, a.error);
+    LeafTile::write(sm, vis_bits, lod_bits, geo, b, a.n, tile == 0, off, a.num_state_sets, a.lods,
                     a.num_geometries, a.num_lods, a.cmds, a.counts, a.error);
     if (t == 0) finish_pass(s.ctl);
 }
@@ -203,11 +205,17 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
+// StateSet offsets are staged in shared memory up to this many entries.
+constexpr uint32_t kLeafOffsetCap = 4096;
+
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream)
 {
     if (a.n == 0) return cudaSuccess;
     const uint32_t grid = (a.n + kLeafTile - 1) / kLeafTile;
-    leaf_kernel<true><<<grid, kLeafThreads, 0, stream>>>(a, s);
+    LeafArgs b = a;
+    b.off_cap = kLeafOffsetCap;
+    const size_t smem = (a.num_state_sets + 1 <= kLeafOffsetCap) ? (a.num_state_sets + 1) * sizeof(uint32_t) : 0;
+    leaf_kernel<true><<<grid, kLeafThreads, smem, stream>>>(b, s);
     return cudaGetLastError();
 }
 

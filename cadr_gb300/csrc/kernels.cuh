@@ -37,6 +37,7 @@ struct LeafArgs {
     uint32_t* error;              // device-visible error word
     uint64_t spin_limit_ns;
     uint32_t fault;
+    uint32_t off_cap;             // offsets staged in shared memory when S+1 <= off_cap (set by the launcher)
     ViewConst view;
 };
 
@@ -76,11 +77,6 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 // Fused plain pass over the leaf level: propagate, transform spheres, cull,
 // select LOD, compact per StateSet.
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream);
-
-// The same pass as a persistent double-buffered TMA kernel (1 CTA per SM,
-// tiles of leaf_tma_tile() drawables); used by cadr_cull.
-cudaError_t launch_leaf_cull_tma(const LeafArgs& a, Scratch& s, int num_sms, int device, cudaStream_t stream);
-uint32_t leaf_tma_tile();
 
 // Batched sphere cull: one persistent launch over all (view, tile) items.
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items,

@@ -285,7 +285,7 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
         if (e != cudaSuccess) return cuda_fail(e, "cull: clear counts");
         return CADR_OK;
     }
-    const uint64_t tiles = (sc->desc.num_drawables + leaf_tma_tile() - 1) / leaf_tma_tile();
+    const uint64_t tiles = (sc->desc.num_drawables + kLeafTile - 1) / kLeafTile;
     st = scratch_reserve(ctx, ctx->scratch, tiles);
     if (st != CADR_OK) return st;
     if (ctx->pass_recorded) {
@@ -306,7 +306,7 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     a.counts = counts;
     a.marginal = marginal;
     a.view = to_view_const(*view);
-    e = launch_leaf_cull_tma(a, ctx->scratch, ctx->num_sms, ctx->device, s);
+    e = launch_leaf_cull(a, ctx->scratch, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull: launch");
     if (fev) {
         cudaEventRecord(fev[2], s);
