@@ -48,6 +48,12 @@ def parse():
     ap.add_argument("--n", type=int, default=16_777_216, help="drawables of the C2 scene")
     ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (default: min(steps, 50))")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form (C4) measurement")
+    ap.add_argument("--form", default="plain", choices=["plain", "serving"])
+    ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of request stream")
+    ap.add_argument("--serving-scenes", type=int, default=64)
+    ap.add_argument("--inflight", type=int, default=4, help="serving: batches in flight")
     return ap.parse_args()
 
 
@@ -147,6 +153,231 @@ def step_algorithmic_bytes(sc, visible: int) -> int:
     return b
 
 
+def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32):
+    """Batched form on C4: 256 views (8 per scene) over 32 scenes of
+    1,000 .. 2,000,000 drawables, culled by one persistent launch replayed
+    from a captured CUDA graph with the autotuned shape, against 256
+    sequential plain passes (each a full pass of its scene).  Returns the
+    timings and whether all 256 outputs are bit-identical."""
+    import torch
+    from cadr_gb300 import lib, scenes
+    from oracle import bind
+    scs = scenes.config4(num_scenes=num_scenes)
+    dss = [lib.DeviceScene(ctx, sc) for sc in scs]
+    for ds in dss:
+        ds.propagate(world_spheres=True)
+    items, plain_outs = [], []
+    for sc, ds in zip(scs, dss):
+        for v in sc.views:
+            items.append((ds, v, lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False)))
+            plain_outs.append(lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False))
+    arr = lib.batch_views(items)
+    tuning, tune_ms = lib.autotune_batched(ctx, arr, reps=3)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def plain_step():
+        k = 0
+        for sc, ds in zip(scs, dss):
+            for v in sc.views:
+                o = plain_outs[k]
+                lib.check(ctx.lib.cadr_cull(ds.handle, np.ascontiguousarray(v).ctypes.data, o.cmds.ptr,
+                                            o.counts.ptr, None, None))
+                k += 1
+
+    def batched_step():
+        lib.cull_batched(ctx, arr, None, use_graph=True)
+
+    res = {}
+    for name, fn in (("plain", plain_step), ("batched", batched_step)):
+        for _ in range(warmup):
+            fn()
+        ctx.sync()
+        l0 = ctx.launch_count
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        ctx.sync()
+        res[name] = (e0.elapsed_time(e1) / steps, (ctx.launch_count - l0) // steps)
+    ctx.check_device_error()
+    identical = True
+    for (ds, v, ob), op in zip(items, plain_outs):
+        gb, gp = ob.fetch(), op.fetch()
+        off = ds.host.state_set_offsets
+        identical &= bool(np.array_equal(gb["counts"], gp["counts"]) and np.array_equal(
+            bind.valid_cmds(gb["cmds"], gb["counts"], off).view(np.uint8),
+            bind.valid_cmds(gp["cmds"], gp["counts"], off).view(np.uint8)))
+    view_items = sum(sc.n * len(sc.views) for sc in scs)
+    return {
+        "workload": f"C4: {len(items)} views over {len(scs)} scenes of {min(s.n for s in scs)}.."
+                    f"{max(s.n for s in scs)} drawables (log-uniform), 4 perspective + 4 ortho cascades each",
+        "view_drawables": view_items,
+        "plain_ms": res["plain"][0], "batched_ms": res["batched"][0],
+        "speedup": res["plain"][0] / res["batched"][0],
+        "batched_gitems_per_s": view_items / (res["batched"][0] / 1e3) / 1e9,
+        "plain_gitems_per_s": view_items / (res["plain"][0] / 1e3) / 1e9,
+        "launches_per_step": {"plain": res["plain"][1], "batched": res["batched"][1]},
+        "tuning": {"block_threads": tuning.block_threads, "items_per_thread": tuning.items_per_thread,
+                   "ctas_per_sm": tuning.ctas_per_sm, "autotune_ms": tune_ms},
+        "bit_identical": identical,
+        "note": "batched: scenes propagated once (world spheres), one persistent launch over (view, tile) "
+                "items from a captured CUDA graph; plain: 256 full passes",
+    }
+
+
+def run_tier_a(ctx, n: int, steps: int, warmup: int, peak: float):
+    """Tier A (the reference shader's pass) on n drawables packed in StateSet
+    order, 4,096 geometries, one MatrixList and one drawable-data allocation
+    per drawable: 3-level handle tables.  Checked in full against the
+    oracle.  148 algorithmic bytes per drawable."""
+    import torch
+    from cadr_gb300 import lib, tier_a
+    from oracle import bind
+    # The image holds absolute device addresses: size it first, then build it
+    # for the buffer it will live in.
+    dev = ctx.alloc(tier_a.image_size(n, num_geometries=4096) + 4096)
+    im = tier_a.build(n, seed=7, base=dev.ptr, num_geometries=4096)
+    ref_ind, ref_ptr = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables,
+                                              threads=bind.max_threads())
+    ctx.upload(dev, im.image)
+    d = ctx.to_device(im.drawables)
+    ind, ptr = ctx.alloc(n * 16), ctx.alloc(n * 32)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(warmup):
+        ctx.process_drawables(im.level, im.root, d, n, ind, ptr)
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.process_drawables(im.level, im.root, d, n, ind, ptr)
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / steps
+    same = bool(np.array_equal(ctx.download(ind, np.uint32, (n, 4)), ref_ind) and
+                np.array_equal(ctx.download(ptr, np.uint64, (n, 4)), ref_ptr))
+    gbs = n * 148 / (ms / 1e3) / 1e9
+    return {"workload": f"{n} drawables, 4,096 geometries, {im.num_handles} handles (level {im.level} tables)",
+            "gdrawables_per_s": n / (ms / 1e3) / 1e9, "ms": ms, "algorithmic_bytes_per_drawable": 148,
+            "achieved_gbs": gbs, "frac_of_peak": gbs / peak, "bit_exact_vs_oracle": same}
+
+
+def run_serving(args):
+    """Serving form on C5: 64 resident scenes (10,000 .. 8,000,000 drawables,
+    log-uniform, built as C2 with seeds 4000+i), a Poisson stream of cull
+    requests (rate --rate, 1-4 views each, random cameras with fovY
+    U[30,90]), continuous batching with a 200 us window; beside it the plain
+    loop that serves one request per launch in arrival order.  Latency is
+    submit -> completion; throughput counts (view, drawable) pairs."""
+    import time as _t
+    from cadr_gb300 import build, lib, rng, scenes
+    from oracle import bind
+    build.build()
+    t0 = _t.time()
+    scs = scenes.config5_scenes(num_scenes=args.serving_scenes)
+    gen_s = _t.time() - t0
+    ctx = lib.Context(0)
+    dss = [lib.DeviceScene(ctx, sc) for sc in scs]
+    for ds in dss:
+        ds.propagate(world_spheres=True)
+    ctx.sync()
+    pool = np.concatenate([scenes.random_view(4, k) for k in range(2048)])
+    # The request stream: exponential inter-arrival times, scene and views
+    # drawn from the seeded stream.
+    st = rng.Stream(4, "serving.requests")
+    nreq = int(args.rate * args.duration)
+    idx = np.arange(nreq, dtype=np.uint64)
+    gaps = -np.log(1.0 - st.uniform(idx * np.uint64(4)))  / args.rate
+    arrive = np.cumsum(gaps)
+    scene_of = st.integers(idx * np.uint64(4) + np.uint64(1), 0, len(scs) - 1)
+    nview = st.integers(idx * np.uint64(4) + np.uint64(2), 1, 4)
+    view0 = st.integers(idx * np.uint64(4) + np.uint64(3), 0, len(pool) - 4)
+
+    def summarize(lat, items, wall):
+        lat = np.asarray(lat)
+        return {"requests": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+                "gdrawables_per_s": items / wall / 1e9, "wall_s": wall}
+
+    # Continuous batching.
+    srv = lib.Server(ctx, max_inflight=args.inflight, max_batch_views=64, window_ns=200_000)
+    lat, items, sub_t, done = [], 0, {}, 0
+    start = _t.perf_counter()
+    k = 0
+    while done < nreq:
+        now = _t.perf_counter() - start
+        while k < nreq and arrive[k] <= now:
+            v = pool[view0[k]:view0[k] + nview[k]]
+            rid = srv.submit(dss[scene_of[k]], v)
+            sub_t[rid] = k
+            k += 1
+            now = _t.perf_counter() - start
+        for r in srv.poll():
+            assert r.status == lib.OK
+            lat.append((r.complete_ns - r.submit_ns) * 1e-9)
+            j = sub_t.pop(r.request_id)
+            items += scs[scene_of[j]].n * int(nview[j])
+            srv.release(r.request_id)
+            done += 1
+    wall = _t.perf_counter() - start
+    batched = summarize(lat, items, wall)
+    srv.close()
+
+    # Plain loop: one request per launch, first come first served, over the
+    # first 20 s of the same stream (it falls behind the arrivals, so its
+    # queue grows for as long as it runs).
+    outs = [lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False) for sc in scs for _ in range(4)]
+    lat, items = [], 0
+    nplain = int(min(nreq, args.rate * min(args.duration, 20.0)))
+    start = _t.perf_counter()
+    for j in range(nplain):
+        now = _t.perf_counter() - start
+        if now < arrive[j]:
+            _t.sleep(max(0.0, arrive[j] - now - 50e-6))
+            while _t.perf_counter() - start < arrive[j]:
+                pass
+        s = scene_of[j]
+        v = pool[view0[j]:view0[j] + nview[j]]
+        arr = lib.batch_views([(dss[s], v[q:q + 1], outs[4 * s + q]) for q in range(nview[j])])
+        lib.cull_batched(ctx, arr, None, use_graph=False)
+        ctx.sync()
+        lat.append(_t.perf_counter() - start - arrive[j])
+        items += scs[s].n * int(nview[j])
+    wall = _t.perf_counter() - start
+    plain = summarize(lat, items, wall)
+
+    # Bit-exactness of served results against the plain pass (sample).
+    srv = lib.Server(ctx, max_inflight=args.inflight, max_batch_views=64, window_ns=200_000)
+    ok = True
+    for j in range(0, min(nreq, 64)):
+        s = scene_of[j]
+        v = pool[view0[j]:view0[j] + 1]
+        rid = srv.submit(dss[s], v)
+        srv.drain()
+        res = {r.request_id: r for r in srv.poll()}[rid]
+        counts = ctx.download(res.counts[0], np.uint32, (scs[s].num_state_sets,))
+        cmds = ctx.download(res.cmds[0], scenes.CMD_DTYPE, (scs[s].n,))
+        o = lib.CullOutputs(ctx, scs[s].n, scs[s].num_state_sets)
+        dss[s].cull(v, o)
+        ctx.sync()
+        alone = o.fetch()
+        ok &= bool(np.array_equal(counts, alone["counts"]) and np.array_equal(
+            bind.valid_cmds(cmds, counts, scs[s].state_set_offsets).view(np.uint8),
+            bind.valid_cmds(alone["cmds"], alone["counts"], scs[s].state_set_offsets).view(np.uint8)))
+        srv.release(rid)
+    srv.close()
+    line = {
+        "metric": "serving: Gdrawables/s and p50/p99 latency", "form": "serving",
+        "value": batched["gdrawables_per_s"], "unit": "Gdrawables/s", "n_gpus": 1, "higher_is_better": True,
+        "config": {"workload": f"C5: {len(scs)} resident scenes, {sum(s.n for s in scs)} drawables total, "
+                               f"Poisson {args.rate:.0f} req/s for {args.duration:.0f} s, 1-4 views, 200 us window",
+                   "inflight_batches": args.inflight},
+        "continuous_batching": batched, "plain_one_request_per_launch": plain,
+        "served_equals_plain_pass": ok, "scene_generation_s": gen_s, "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, sc, world, rank):
     """CPU restatement of the pass (the oracle) on all host cores."""
     from oracle import bind
@@ -180,6 +411,10 @@ def main():
     args = parse()
     world, rank, local = dist_env()
     if args.impl == "reference" and rank != 0:
+        return
+    if args.form == "serving":
+        if rank == 0:
+            run_serving(args)
         return
     from cadr_gb300 import scenes
     t0 = time.time()
@@ -325,6 +560,9 @@ def main():
         "clocks": clk,
         "scene_generation_s": gen_s,
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(ctx, steps=max(3, min(args.steps, 20)), warmup=3)
+        line["tier_a"] = run_tier_a(ctx, args.n, steps=max(3, min(args.steps, 50)), warmup=3, peak=peak)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import bind
         import oracle

@@ -55,6 +55,28 @@ class TierAImage:
     num_handles: int
 
 
+def _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles):
+    """Handle count, table depth and region sizes of an image."""
+    H = 3 * G + n + (n if with_drawable_data else 0) + extra_handles
+    level = handle_level(H)
+    n_llt = H // TABLE + 1                      # last-level tables
+    n_rt = 0 if level < 3 else (H >> 22) + 1    # level-1 routing tables (level 3 only)
+    n_tables = n_llt + (1 if level == 2 else 0) + (n_rt + 1 if level == 3 else 0)
+    tables_bytes = n_tables * TABLE * 8
+    prims_bytes = G * prims_per_geometry * 8
+    ml_stride = 64 + 64 * matrices_per_list
+    ml_off = (tables_bytes + prims_bytes + 255) & ~255
+    size = ml_off + n * ml_stride
+    return H, level, n_llt, n_rt, n_tables, tables_bytes, prims_bytes, ml_stride, ml_off, size
+
+
+def image_size(n: int, num_geometries: int | None = None, prims_per_geometry: int = 3,
+               with_drawable_data: bool = True, matrices_per_list: int = 1, extra_handles: int = 0) -> int:
+    """Bytes of the image build() makes for the same arguments."""
+    G = num_geometries or max(1, min(n, 4096))
+    return _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles)[-1]
+
+
 def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries: int | None = None,
           prims_per_geometry: int = 3, with_drawable_data: bool = True,
           matrices_per_list: int = 1, extra_handles: int = 0) -> TierAImage:
@@ -71,19 +93,9 @@ def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries:
     h_prims = h_vertex + 2
     h_ml = 1 + 3 * G + np.arange(n, dtype=np.uint64)
     h_dd = (1 + 3 * G + n + np.arange(n, dtype=np.uint64)) if with_drawable_data else np.zeros(n, np.uint64)
-    H = 3 * G + n + (n if with_drawable_data else 0) + extra_handles
-    level = handle_level(H)
-
-    # Region sizes.
-    n_llt = H // TABLE + 1                      # last-level tables
-    n_rt = 0 if level < 3 else (H >> 22) + 1    # level-1 routing tables (level 3 only)
-    n_tables = n_llt + (1 if level == 2 else 0) + (n_rt + 1 if level == 3 else 0)
-    tables_bytes = n_tables * TABLE * 8
+    H, level, n_llt, n_rt, n_tables, tables_bytes, prims_bytes, ml_stride, ml_off, size = _layout(
+        n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles)
     prims_off = tables_bytes
-    prims_bytes = G * prims_per_geometry * 8
-    ml_stride = 64 + 64 * matrices_per_list
-    ml_off = (prims_off + prims_bytes + 255) & ~255
-    size = ml_off + n * ml_stride
     img = np.zeros(size, np.uint8)
     tables = img[:tables_bytes].view(np.uint64).reshape(n_tables, TABLE)
 
