@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (default: min(steps, 50))")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form (C4) measurement")
-    ap.add_argument("--form", default="plain", choices=["plain", "serving"])
+    ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a"])
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of request stream")
     ap.add_argument("--serving-scenes", type=int, default=64)
@@ -415,6 +415,14 @@ def main():
     if args.form == "serving":
         if rank == 0:
             run_serving(args)
+        return
+    if args.form == "tier-a":
+        from cadr_gb300 import build, lib
+        build.build()
+        import oracle
+        oracle.build(with_ref=False)
+        ctx = lib.Context(local)
+        print(json.dumps({"form": "tier-a", **run_tier_a(ctx, args.n, args.steps, args.warmup, measured_peak()[0])}))
         return
     from cadr_gb300 import scenes
     t0 = time.time()
