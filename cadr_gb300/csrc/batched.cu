@@ -82,17 +82,24 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         const uint32_t b = (item - job.first_item) * (uint32_t)T::SIZE;
         uint32_t vis_bits = 0, lod_bits = 0;
         uint32_t geo[IPT];
+        float4 wsv[IPT];
+        // Every item's inputs in flight together, then the arithmetic.
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const uint32_t i = b + (uint32_t)(j * THREADS + t);
+            const uint32_t ic = i < job.n ? i : 0u;
+            wsv[j] = job.n ? ld_nc_f4(job.world_sphere + ic) : make_float4(0.f, 0.f, 0.f, 0.f);
+            geo[j] = job.n ? ld_nc_u32(job.geometry + ic) : 0u;
+        }
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
             const uint32_t i = b + (uint32_t)(j * THREADS + t);
             bool visible = false, marginal = false;
             uint32_t lod = 0;
-            geo[j] = 0;
-            if (i < job.n) {
-                const float4 ws = ld_nc_f4(job.world_sphere + i);
-                geo[j] = ld_nc_u32(job.geometry + i);
-                classify(job.view, ws, job.num_lods, visible, marginal, lod);
-            }
+            if (i < job.n)
+                classify(job.view, wsv[j], job.num_lods, visible, marginal, lod);
+            else
+                geo[j] = 0;
             const uint32_t vb = __ballot_sync(~0u, visible);
             const uint32_t mb = __ballot_sync(~0u, marginal);
             const uint32_t word0 = b + (uint32_t)(j * THREADS + warp * kWarp);

@@ -177,6 +177,20 @@ struct Tile {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
         const uint32_t start_f = offsets[rf];
+        // All LOD-table gathers first, so that their L2 round trips overlap
+        // instead of each one waiting behind the previous command's stores.
+        uint4 ent[IPT];
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            ent[j] = make_uint4(0u, 0u, 0u, 0u);
+            if (!((vis_bits >> j) & 1u)) continue;
+            uint32_t g = geo[j];
+            if (g >= G) {
+                atomicOr(error, CADR_DEVERR_BAD_INDEX);
+                g = 0;
+            }
+            ent[j] = __ldg(lods + (size_t)g * L + ((lod_bits >> (2 * j)) & 3u));
+        }
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
             if (!((vis_bits >> j) & 1u)) continue;
@@ -185,12 +199,7 @@ struct Tile {
             const uint32_t start = (r == rf) ? start_f : offsets[r];
             const uint32_t ei = excl(sm, i - b);
             const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
-            uint32_t g = geo[j];
-            if (g >= G) {
-                atomicOr(error, CADR_DEVERR_BAD_INDEX);
-                g = 0;
-            }
-            const uint4 e = __ldg(lods + (size_t)g * L + ((lod_bits >> (2 * j)) & 3u));
+            const uint4 e = ent[j];
             uint32_t* c = cmds + (size_t)slot * 5;
             c[0] = e.x;
             c[1] = 1u;
