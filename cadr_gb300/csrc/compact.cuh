@@ -79,7 +79,8 @@ struct Tile {
     struct Smem {
         uint32_t ballot[IPT][NW];
         uint32_t prefix[NC];
-        uint32_t info[8];  // 0 item, 1 epoch, 2 carry, 3 total, 4 first region, 5 last region
+        uint32_t info[8];  // 0 item, 1 epoch, 2 carry, 3 total, 4 first region, 5 last region,
+                           // 6 published value, 7 published head flag
     };
 
     // Tile-local exclusive prefix of visible items at tile position q (0..SIZE).
@@ -131,6 +132,49 @@ struct Tile {
         __syncthreads();
     }
 
+    // One lane of warp 0, after scan(): publish the tile's aggregate (the
+    // scan's first item publishes its inclusive prefix at once) and keep the
+    // published value and head flag in info[6], info[7] for resolve().
+    __device__ static __forceinline__ void publish(Smem& sm, uint64_t* __restrict__ states, int64_t item,
+                                                   int64_t first, const uint32_t* __restrict__ offsets, uint32_t b,
+                                                   uint32_t fault)
+    {
+        const uint32_t total = sm.info[3];
+        const uint32_t last_start = offsets[sm.info[5]];
+        const uint32_t head = last_start >= b ? 1u : 0u;
+        const uint32_t val = head ? total - excl(sm, last_start - b) : total;
+        sm.info[6] = val;
+        sm.info[7] = head;
+        if (item == first) {
+            if (fault != CADR_FAULT_SKIP_FIRST_TILE_PUBLISH)
+                store_relaxed_u64(states + item, pack_status(sm.info[1], kStatusPrefix, 1u, val));
+        } else {
+            store_relaxed_u64(states + item, pack_status(sm.info[1], kStatusAgg, head, val));
+        }
+    }
+
+    // Warp 0, after publish() and a barrier or in the publishing warp: look
+    // back and publish the inclusive prefix; carry in info[2] (visible to the
+    // CTA after the caller's next __syncthreads()).
+    __device__ static __forceinline__ void resolve(Smem& sm, uint64_t* __restrict__ states, int64_t item,
+                                                   int64_t first, uint64_t limit_ns, uint32_t* error)
+    {
+        const int lane = threadIdx.x & 31;
+        __syncwarp();
+        uint32_t carry = 0;
+        bool timed_out = false;
+        if (item != first) {
+            const uint32_t epoch = sm.info[1], val = sm.info[6], head = sm.info[7];
+            carry = warp_lookback(states, item, first, epoch, limit_ns, timed_out);
+            if (lane == 0)
+                store_relaxed_u64(states + item, pack_status(epoch, kStatusPrefix, head, head ? val : carry + val));
+        }
+        if (lane == 0) {
+            sm.info[2] = carry;
+            if (timed_out) atomicOr(error, CADR_DEVERR_LOOKBACK_TIMEOUT);
+        }
+    }
+
     // Warp 0: publish the tile aggregate, look back, publish the inclusive
     // prefix.  `item` indexes `states`; items in [first, item) precede it in
     // the same scan.  Ends with __syncthreads(); carry in info[2].
@@ -138,30 +182,30 @@ struct Tile {
                                                     int64_t first, const uint32_t* __restrict__ offsets, uint32_t b,
                                                     uint64_t limit_ns, uint32_t fault, uint32_t* error)
     {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (warp == 0) {
-            const uint32_t total = sm.info[3];
-            const uint32_t epoch = sm.info[1];
-            const uint32_t last_start = offsets[sm.info[5]];
-            const uint32_t head = last_start >= b ? 1u : 0u;
-            const uint32_t val = head ? total - excl(sm, last_start - b) : total;
-            uint32_t carry = 0;
-            bool timed_out = false;
-            if (item == first) {
-                if (lane == 0 && fault != CADR_FAULT_SKIP_FIRST_TILE_PUBLISH)
-                    store_relaxed_u64(states + item, pack_status(epoch, kStatusPrefix, 1u, val));
-            } else {
-                if (lane == 0) store_relaxed_u64(states + item, pack_status(epoch, kStatusAgg, head, val));
-                carry = warp_lookback(states, item, first, epoch, limit_ns, timed_out);
-                if (lane == 0)
-                    store_relaxed_u64(states + item, pack_status(epoch, kStatusPrefix, head, head ? val : carry + val));
-            }
-            if (lane == 0) {
-                sm.info[2] = carry;
-                if (timed_out) atomicOr(error, CADR_DEVERR_LOOKBACK_TIMEOUT);
-            }
+        if ((threadIdx.x >> 5) == 0) {
+            if ((threadIdx.x & 31) == 0) publish(sm, states, item, first, offsets, b, fault);
+            resolve(sm, states, item, first, limit_ns, error);
         }
         __syncthreads();
+    }
+
+    // Every thread: the LOD-table entries of its visible items, all issued
+    // together so that their L2 round trips overlap.
+    __device__ static __forceinline__ void gather(uint32_t vis_bits, uint32_t lod_bits, const uint32_t (&geo)[IPT],
+                                                  const uint4* __restrict__ lods, uint32_t G, uint32_t L,
+                                                  uint32_t* error, uint4 (&ent)[IPT])
+    {
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            ent[j] = make_uint4(0u, 0u, 0u, 0u);
+            if (!((vis_bits >> j) & 1u)) continue;
+            uint32_t g = geo[j];
+            if (g >= G) {
+                atomicOr(error, CADR_DEVERR_BAD_INDEX);
+                g = 0;
+            }
+            ent[j] = __ldg(lods + (size_t)g * L + ((lod_bits >> (2 * j)) & 3u));
+        }
     }
 
     // Every thread: write the commands of its visible items and the counts
@@ -174,32 +218,40 @@ struct Tile {
                                                  uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts,
                                                  uint32_t* error)
     {
+        uint4 ent[IPT];
+        gather(vis_bits, lod_bits, geo, lods, G, L, error, ent);
+        write_ent(sm, vis_bits, ent, b, n, first_tile, offsets, S, cmds, counts);
+    }
+
+    // write() with the LOD entries already gathered.
+    __device__ static __forceinline__ void write_ent(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[IPT],
+                                                     uint32_t b, uint32_t n, bool first_tile,
+                                                     const uint32_t* __restrict__ offsets, uint32_t S,
+                                                     uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts)
+    {
+        write_cmds<0, IPT>(sm, vis_bits, ent, b, offsets, cmds);
+        write_counts(sm, b, n, first_tile, offsets, S, counts);
+    }
+
+    // The commands of the thread's visible items in rows [J0, J1); bit j of
+    // vis_bits and ent[j - J0] belong to row j.
+    template <int J0, int J1>
+    __device__ static __forceinline__ void write_cmds(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[J1 - J0],
+                                                      uint32_t b, const uint32_t* __restrict__ offsets,
+                                                      uint32_t* __restrict__ cmds)
+    {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
         const uint32_t start_f = offsets[rf];
-        // All LOD-table gathers first, so that their L2 round trips overlap
-        // instead of each one waiting behind the previous command's stores.
-        uint4 ent[IPT];
 #pragma unroll
-        for (int j = 0; j < IPT; j++) {
-            ent[j] = make_uint4(0u, 0u, 0u, 0u);
-            if (!((vis_bits >> j) & 1u)) continue;
-            uint32_t g = geo[j];
-            if (g >= G) {
-                atomicOr(error, CADR_DEVERR_BAD_INDEX);
-                g = 0;
-            }
-            ent[j] = __ldg(lods + (size_t)g * L + ((lod_bits >> (2 * j)) & 3u));
-        }
-#pragma unroll
-        for (int j = 0; j < IPT; j++) {
+        for (int j = J0; j < J1; j++) {
             if (!((vis_bits >> j) & 1u)) continue;
             const uint32_t i = b + (uint32_t)(j * THREADS + t);
             const uint32_t r = (rf == rl) ? rf : region_of(offsets, rf, rl + 1, i);
             const uint32_t start = (r == rf) ? start_f : offsets[r];
             const uint32_t ei = excl(sm, i - b);
             const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
-            const uint4 e = ent[j];
+            const uint4 e = ent[j - J0];
             uint32_t* c = cmds + (size_t)slot * 5;
             c[0] = e.x;
             c[1] = 1u;
@@ -207,6 +259,16 @@ struct Tile {
             c[3] = e.z;
             c[4] = i;
         }
+    }
+
+    // Every thread: the counts of the regions ending in this tile (the
+    // scan's first tile also writes the zero counts of empty regions).
+    __device__ static __forceinline__ void write_counts(const Smem& sm, uint32_t b, uint32_t n, bool first_tile,
+                                                        const uint32_t* __restrict__ offsets, uint32_t S,
+                                                        uint32_t* __restrict__ counts)
+    {
+        const int t = threadIdx.x;
+        const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
         const uint32_t e_tile = min(b + (uint32_t)SIZE, n);
         for (uint32_t k = rf + (uint32_t)t; k <= rl; k += THREADS) {
             const uint32_t sk = offsets[k], ek = offsets[k + 1];

@@ -61,7 +61,10 @@ struct ViewJob {
 };
 
 constexpr int kLeafThreads = 256;
-constexpr int kLeafIpt = 8;
+#ifndef CADR_LEAF_IPT
+#define CADR_LEAF_IPT 8
+#endif
+constexpr int kLeafIpt = CADR_LEAF_IPT;
 constexpr int kLeafTile = kLeafThreads * kLeafIpt;
 constexpr int kPropThreads = 256;
 

@@ -23,11 +23,11 @@ using namespace cadr;
 namespace cadr {
 namespace {
 
-// Largest scene the entry point accepts: 16,384 tiles of 2,048 drawables.
-constexpr uint64_t kStaticMaxTiles = 16384;
-constexpr uint64_t kStaticMaxDrawables = kStaticMaxTiles * (uint64_t)kLeafTile;  // 33,554,432
+// Largest scene the entry point accepts, and the tiles it needs.
+constexpr uint64_t kStaticMaxDrawables = 33554432;
+constexpr uint64_t kStaticMaxTiles = (kStaticMaxDrawables + kLeafTile - 1) / kLeafTile;
 constexpr size_t kCtlBytes = 256;  // LookbackCtl, padded to keep the tile states 256-byte aligned
-constexpr size_t kStaticScratchBytes = kCtlBytes + kStaticMaxTiles * sizeof(uint64_t);  // 128 KiB + 256 B
+constexpr size_t kStaticScratchBytes = kCtlBytes + kStaticMaxTiles * sizeof(uint64_t);  // 128 KiB + 256 B for 2,048-drawable tiles
 
 // The scratch.  Host code must not take this symbol's address directly: on
 // the host it names a stand-in, not device memory.  The device address comes

@@ -48,6 +48,9 @@ def test_c1_against_golden_and_oracle(ctx):
     (1, 0, 1, 1, ()), (31, 1, 2, 2, ()), (32, 2, 3, 3, (1,)), (2047, 2, 5, 4, ()),
     (2048, 1, 4, 3, (0, 3)), (2049, 3, 7, 3, (6,)), (5000, 2, 1, 2, ()), (100_003, 3, 64, 3, (5, 17)),
     (40_000, 2, 3000, 3, ()), (70_001, 0, 9, 1, (8,)),
+    # Edges of a warp's 256 drawables, and more StateSets than
+    # the 4,096 offsets staged in shared memory.
+    (255, 1, 2, 2, ()), (256, 2, 3, 3, (2,)), (257, 1, 300, 3, ()), (300_001, 2, 5000, 3, (7, 4999)),
 ])
 def test_edge_cases_against_oracle(ctx, n, levels, S, lods, empty):
     sc = scenes.small_scene(seed=n + 7 * levels, n=n, num_levels=levels, num_state_sets=S, num_lods=lods,
