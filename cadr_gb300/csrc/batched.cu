@@ -30,6 +30,8 @@ struct BatchedState {
     uint32_t key_views = 0, key_items = 0, key_grid = 0;
     cadr_tuning key_tuning = {};
     cudaStream_t key_stream = nullptr;
+    uint64_t key_limit = 0;
+    uint32_t key_fault = 0;
 };
 
 namespace {
@@ -41,7 +43,7 @@ constexpr uint32_t kBatchedOffsetCap = 2048;
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
                                                          uint32_t total_items, const Scratch s, uint32_t* error,
-                                                         uint64_t limit_ns)
+                                                         uint64_t limit_ns, uint32_t fault)
 {
     using T = Tile<THREADS, IPT>;
     __shared__ typename T::Smem sm;
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         }
         __syncthreads();
         T::scan(sm, off, job.num_state_sets, b, job.n);
-        T::lookback(sm, s.tile_state, item, job.first_item, off, b, limit_ns, 0u, error);
+        T::lookback(sm, s.tile_state, item, job.first_item, off, b, limit_ns, fault, error);
         T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, off, job.num_state_sets,
                  job.lods, job.num_geometries, job.num_lods, job.cmds, job.counts, error);
         __syncthreads();
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
     if (t == 0) finish_pass(s.ctl);
 }
 
-using KernelFn = void (*)(const ViewJob*, uint32_t, uint32_t, const Scratch, uint32_t*, uint64_t);
+using KernelFn = void (*)(const ViewJob*, uint32_t, uint32_t, const Scratch, uint32_t*, uint64_t, uint32_t);
 
 template <int TH>
 KernelFn pick_ipt(uint32_t ipt)
@@ -151,13 +153,13 @@ uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread)
 }
 
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items, Scratch& s,
-                                uint32_t* error, uint64_t spin_limit_ns, uint32_t block_threads,
+                                uint32_t* error, uint64_t spin_limit_ns, uint32_t fault, uint32_t block_threads,
                                 uint32_t items_per_thread, uint32_t grid, cudaStream_t stream)
 {
     KernelFn k = pick_kernel(block_threads, items_per_thread);
     if (!k) return cudaErrorInvalidValue;
     k<<<grid, block_threads, kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s, error,
-                                                                          spin_limit_ns);
+                                                                          spin_limit_ns, fault);
     return cudaGetLastError();
 }
 
@@ -289,7 +291,8 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
 
     if (use_graph) {
         const bool same = B.exec && B.key_views == num_views && B.key_items == total && B.key_grid == grid &&
-                          B.key_stream == s && std::memcmp(&B.key_tuning, &tu, sizeof(tu)) == 0;
+                          B.key_stream == s && B.key_limit == ctx->spin_limit_ns && B.key_fault == ctx->fault &&
+                          std::memcmp(&B.key_tuning, &tu, sizeof(tu)) == 0;
         if (!same) {
             if (B.exec) cudaGraphExecDestroy(B.exec);
             if (B.graph) cudaGraphDestroy(B.graph);
@@ -299,7 +302,7 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
             if (e != cudaSuccess) return cuda_fail(e, "cull_batched: begin capture");
             cudaError_t e1 = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
             cudaError_t e2 = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error,
-                                                 ctx->spin_limit_ns, tu.block_threads, tu.items_per_thread, grid, s);
+                                                 ctx->spin_limit_ns, ctx->fault, tu.block_threads, tu.items_per_thread, grid, s);
             e = cudaStreamEndCapture(s, &B.graph);
             if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess) {
                 if (B.graph) cudaGraphDestroy(B.graph);
@@ -313,6 +316,8 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
             B.key_grid = grid;
             B.key_tuning = tu;
             B.key_stream = s;
+            B.key_limit = ctx->spin_limit_ns;
+            B.key_fault = ctx->fault;
         }
         e = cudaGraphLaunch(B.exec, s);
         if (e != cudaSuccess) return cuda_fail(e, "cull_batched: graph launch");
@@ -320,7 +325,7 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
         e = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) return cuda_fail(e, "cull_batched: job copy");
         e = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error, ctx->spin_limit_ns,
-                                tu.block_threads, tu.items_per_thread, grid, s);
+                                ctx->fault, tu.block_threads, tu.items_per_thread, grid, s);
         if (e != cudaSuccess) return cuda_fail(e, "cull_batched: launch");
     }
     ctx->launches++;

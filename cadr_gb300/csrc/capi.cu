@@ -38,6 +38,22 @@ cadr_status cuda_fail(cudaError_t e, const char* what)
     return fail(CADR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+cadr_status scratch_reserve_planes(cadr_context* ctx, Scratch& s, uint64_t words)
+{
+    if (words <= s.plane_words) return CADR_OK;
+    // Passes still in flight may use the old area.
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "scratch: synchronize");
+    if (s.planes) cudaFree(s.planes);
+    s.planes = nullptr;
+    s.plane_words = 0;
+    e = cudaMalloc(&s.planes, words * sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(e, "scratch: planes");
+    s.plane_words = words;
+    (void)ctx;
+    return CADR_OK;
+}
+
 cadr_status scratch_reserve(cadr_context* ctx, Scratch& s, uint64_t tiles)
 {
     if (tiles <= s.capacity && s.launches < (1ull << 28)) return CADR_OK;
@@ -73,6 +89,7 @@ void scratch_release(Scratch& s)
 {
     if (s.tile_state) cudaFree(s.tile_state);
     if (s.ctl) cudaFree(s.ctl);
+    if (s.planes) cudaFree(s.planes);
     s = Scratch{};
 }
 

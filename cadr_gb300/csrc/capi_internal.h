@@ -60,6 +60,8 @@ extern thread_local std::string g_last_error;
 cadr_status fail(cadr_status s, const char* fmt, ...);
 cadr_status cuda_fail(cudaError_t e, const char* what);
 cadr_status scratch_reserve(cadr_context* ctx, Scratch& s, uint64_t tiles);
+// Grows s.planes to at least `words` (after a device-wide synchronisation).
+cadr_status scratch_reserve_planes(cadr_context* ctx, Scratch& s, uint64_t words);
 void scratch_release(Scratch& s);
 cadr_status upload_bytes(cadr_context* ctx, void* dst, const void* src, size_t bytes, cudaStream_t stream);
 cudaStream_t pick_stream(cadr_context* ctx, cadr_stream s);

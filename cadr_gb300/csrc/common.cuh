@@ -160,6 +160,14 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic
+// stream serialization may start before the kernel ahead of it on the
+// stream has finished; grid_dependency_wait() returns when that kernel has
+// completed and its memory writes are visible.  grid_dependents_launch()
+// lets the next such kernel start now.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dependents_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Bounded wait on phase `parity`; returns false (after limit_ns) when the
 // barrier never completed.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)

@@ -1,16 +1,17 @@
-// cull.cu - Tier B kernels: hierarchy propagation, the fused leaf pass
-// (world matrix, bounding sphere, frustum cull, LOD, per-StateSet
-// compaction) and the batched sphere cull.
+// cull.cu - Tier B kernels of the plain pass: hierarchy propagation and
+// the leaf pass (world matrix, bounding sphere, frustum cull, LOD,
+// per-StateSet compaction).
 //
-// Compaction is a single-pass segmented scan with decoupled lookback over
-// dynamically numbered tiles (a tile's predecessors were started before it,
-// so they are resident and its wait always ends); each wait is bounded by a
-// time limit after which the tile records CADR_DEVERR_LOOKBACK_TIMEOUT and
-// continues, so no pass can hang the device.  Output order inside a
-// StateSet region is ascending drawable order: deterministic, no atomics on
-// the output.
+// The leaf pass is a reduce-then-scan over tiles of 2,048 drawables in
+// three launches: the stream kernel computes world matrices, world spheres
+// and the classification, and leaves per tile one (count, region-start)
+// word and per 32 drawables the visibility and LOD bits; one CTA scans the
+// tile words into per-tile carries; the write kernel turns the bits and
+// carries into commands and counts.  No kernel waits for another CTA, so
+// the plain pass has no spin-waits at all.  Output order inside a StateSet
+// region is ascending drawable order: deterministic, no atomics on the
+// output.
 #include <algorithm>
-#include <atomic>
 
 #include "compact.cuh"
 #include "kernels.cuh"
@@ -30,21 +31,7 @@ __device__ __forceinline__ void load_mat(const float4* __restrict__ p, float4& c
 
 using LeafTile = Tile<kLeafThreads, kLeafIpt>;
 
-#ifndef CADR_LEAF_CTAS_PER_SM
-#define CADR_LEAF_CTAS_PER_SM 4
-#endif
-constexpr int kLeafCtasPerSm = CADR_LEAF_CTAS_PER_SM;
-// Rows whose LOD entries one thread holds at a time in the compaction.
-constexpr int kLeafChunk = kLeafIpt < 8 ? kLeafIpt : 8;
-static_assert(kLeafIpt == kLeafChunk || kLeafIpt == 2 * kLeafChunk, "one or two compaction chunks");
-
-// Shared-memory record of a streamed tile that the compaction reads:
-// per item its geometry id and LOD (ballots and scan results are in the
-// tile's LeafTile::Smem).
-struct LeafStash {
-    uint32_t geo[kLeafTile];
-    uint8_t lod[kLeafTile];
-};
+constexpr int kLeafWarps = kLeafThreads / kWarp;
 
 // World matrix records leave through a 2 KB staging block per warp, so
 // that each store instruction of a warp writes 512 contiguous bytes:
@@ -59,19 +46,21 @@ __device__ __forceinline__ uint32_t xpose_pos(uint32_t q) { return q ^ ((q >> 3)
 // Streams the drawables [b, b + kLeafTile): world matrix, world sphere
 // and, with kCull, the classification.  Item j of thread t is drawable
 // b + j*kLeafThreads + t, i.e. lane t%32 of row j of warp t/32; xb is the
-// warp's staging block.  With kCull, visibility ballots go to sm, geometry
-// ids and LODs to st at position j*kLeafThreads + t.
+// warp's staging block.  With kCull, row j's visibility ballot goes to
+// ballot[j][warp] and, with the LOD bits and the marginal flags, to the
+// planes (one word per 32 drawables).
 template <bool kCull>
-__device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, LeafTile::Smem* sm, LeafStash* st,
+__device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint32_t (*ballot)[kLeafWarps],
                                             float4* xb)
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t words = (uint32_t)leaf_plane_stride(a.n);
 #pragma unroll
     for (int j = 0; j < kLeafIpt; j++) {
         const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
         const uint32_t i = i0 + (uint32_t)lane;
         bool visible = false, marginal = false;
-        uint32_t lod = 0, geo = 0;
+        uint32_t lod = 0;
         if (i0 < a.n) {
             // The previous row's reads of xb are done before it is rewritten.
             __syncwarp();
@@ -79,7 +68,6 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, LeafT
                 float4 l0, l1, l2, l3, w0, w1, w2, w3;
                 load_mat(a.local + (size_t)i * 4, l0, l1, l2, l3);
                 const float4 sp = ld_nc_f4(a.sphere + i);
-                if (kCull) geo = ld_nc_u32(a.geometry + i);
                 if (a.parent) {
                     uint32_t p = ld_nc_u32(a.parent + i);
                     if (p >= a.num_parents) {
@@ -118,12 +106,18 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, LeafT
         if (kCull) {
             const uint32_t vb = __ballot_sync(~0u, visible);
             const uint32_t mb = __ballot_sync(~0u, marginal);
+            const uint32_t lb0 = __ballot_sync(~0u, (lod & 1u) != 0u);
+            const uint32_t lb1 = __ballot_sync(~0u, (lod & 2u) != 0u);
             if (lane == 0) {
-                sm->ballot[j][warp] = vb;
-                if (a.marginal && i0 < a.n) a.marginal[i0 >> 5] = mb;
+                ballot[j][warp] = vb;
+                if (i0 < a.n) {
+                    const uint32_t w = i0 >> 5;
+                    a.planes[w] = vb;
+                    a.planes[words + w] = lb0;
+                    a.planes[2 * words + w] = lb1;
+                    if (a.marginal) a.marginal[w] = mb;
+                }
             }
-            st->geo[j * kLeafThreads + t] = geo;
-            st->lod[j * kLeafThreads + t] = (uint8_t)lod;
         }
     }
 }
@@ -131,115 +125,193 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, LeafT
 // Leaf level without culling: one CTA per tile.
 __global__ void __launch_bounds__(kLeafThreads, 4) leaf_propagate_kernel(const LeafArgs a)
 {
-    __shared__ float4 xb[kLeafThreads / kWarp][4 * kWarp];
-    stream_tile<false>(a, blockIdx.x * (uint32_t)kLeafTile, nullptr, nullptr, xb[threadIdx.x >> 5]);
+    __shared__ float4 xb[kLeafWarps][4 * kWarp];
+    stream_tile<false>(a, blockIdx.x * (uint32_t)kLeafTile, nullptr, xb[threadIdx.x >> 5]);
 }
 
-// Visibility bits of the thread's items in a streamed tile (bit j: row j).
-__device__ __forceinline__ uint32_t tile_vis_bits(const LeafTile::Smem& sm)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t v = 0;
-#pragma unroll
-    for (int j = 0; j < kLeafIpt; j++) v |= ((sm.ballot[j][warp] >> lane) & 1u) << j;
-    return v;
-}
+// The tile word of the plain pass's segmented scan: the visible drawables
+// of the tile's last StateSet region that lie in the tile (all of the
+// tile's visible drawables when no region starts in it), and in bit 31
+// whether a region starts in the tile.
+constexpr uint32_t kTileHead = 0x80000000u;
 
-// LOD-table entries of the thread's visible items in rows [J0, J0 + kLeafChunk).
-template <int J0>
-__device__ __forceinline__ void gather_rows(const LeafArgs& a, const LeafStash& st, uint32_t vis_bits,
-                                            uint4 (&ent)[kLeafChunk])
+// Plain pass, launch 1 of 3: one CTA per tile streams its drawables
+// (world matrices, world spheres, classification into the planes) and
+// writes the tile word.  No CTA waits for another.
+__global__ void __launch_bounds__(kLeafThreads, 4) leaf_stream_kernel(const LeafArgs a)
 {
-    const int t = threadIdx.x;
-#pragma unroll
-    for (int j = 0; j < kLeafChunk; j++) {
-        ent[j] = make_uint4(0u, 0u, 0u, 0u);
-        if (!((vis_bits >> (J0 + j)) & 1u)) continue;
-        uint32_t g = st.geo[(J0 + j) * kLeafThreads + t];
-        if (g >= a.num_geometries) {
-            atomicOr(a.error, CADR_DEVERR_BAD_INDEX);
-            g = 0;
-        }
-        ent[j] = __ldg(a.lods + (size_t)g * a.num_lods + st.lod[(J0 + j) * kLeafThreads + t]);
-    }
-}
-
-// The fused plain pass, persistent: every CTA takes tiles from the pass's
-// tile counter (so in ascending order across the grid) until none is left.
-// A tile's aggregate is published as soon as its drawables are streamed;
-// its lookback and command writes are deferred until the CTA has streamed
-// its next tile.  By then the tiles before it have published long ago, so
-// the lookback walks published states instead of waiting for neighbours
-// that are still streaming, and the deferred tile's LOD gathers overlap
-// that walk.  Deferral cannot deadlock: a tile's aggregate waits only for
-// the lookback of a lower tile of the same CTA, which waits only for the
-// aggregates of tiles lower still, and tile 0 publishes its prefix at once.
-// Shared memory: two tile records (current, deferred), the warps' staging
-// blocks, then the staged StateSet offsets.
-__global__ void __launch_bounds__(kLeafThreads, kLeafCtasPerSm) leaf_cull_kernel(const LeafArgs a, const Scratch s)
-{
-    __shared__ LeafTile::Smem sm[2];
-    __shared__ uint32_t s_tile;
-    extern __shared__ __align__(16) uint32_t s_dyn[];
-    LeafStash* stash = reinterpret_cast<LeafStash*>(s_dyn);
-    float4* xbs = reinterpret_cast<float4*>(stash + 2);
-    const int t = threadIdx.x, warp = t >> 5;
-    const uint32_t tiles = (a.n + (uint32_t)kLeafTile - 1) / (uint32_t)kLeafTile;
-    constexpr uint32_t kNone = 0xffffffffu;
-
+    __shared__ float4 xb[kLeafWarps][4 * kWarp];
+    __shared__ uint32_t ballot[kLeafIpt][kLeafWarps];
+    __shared__ uint32_t s_last_start;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t tile = blockIdx.x, b = tile * (uint32_t)kLeafTile;
     if (t == 0) {
-        s_tile = atomicAdd(&s.ctl->tile_counter, 1u);
-        const uint32_t epoch = load_relaxed_u32(&s.ctl->epoch);
-        sm[0].info[1] = epoch;
-        sm[1].info[1] = epoch;
+        // Start of the region holding the tile's last drawable; its search
+        // overlaps the stream.
+        const uint32_t e = min(b + (uint32_t)kLeafTile, a.n);
+        const uint32_t rl = min(region_of(a.offsets, 0, a.num_state_sets + 1, e - 1), a.num_state_sets - 1);
+        s_last_start = a.offsets[rl];
     }
-    const uint32_t* off = stage_offsets(reinterpret_cast<uint32_t*>(xbs + kLeafThreads * 4), a.off_cap, a.offsets,
-                                        a.num_state_sets);
+    stream_tile<true>(a, b, ballot, xb[warp]);
     __syncthreads();
-    uint32_t tile = s_tile, pend = kNone;
-    int p = 0;
-    for (;;) {
-        const bool cur = tile < tiles;
-        const uint32_t b = tile * (uint32_t)kLeafTile;
-        if (cur) {
-            stream_tile<true>(a, b, &sm[p], &stash[p], xbs + warp * 4 * kWarp);
-            __syncthreads();
-            LeafTile::scan(sm[p], off, a.num_state_sets, b, a.n);
+    if (warp == 0) {
+        // Ballot k covers the tile's drawables [32k, 32k + 32).
+        const uint32_t ls = s_last_start;
+        const bool head = ls >= b;
+        const uint32_t q = head ? ls - b : 0u;
+        uint32_t total = 0, before = 0;
+#pragma unroll
+        for (int h = 0; h < (kLeafIpt * kLeafWarps) / kWarp; h++) {
+            const uint32_t k = (uint32_t)(lane + h * kWarp);
+            const uint32_t v = ballot[k / kLeafWarps][k % kLeafWarps];
+            total += __popc(v);
+            if (32u * k + 32u <= q)
+                before += __popc(v);
+            else if (32u * k < q)
+                before += __popc(v & ((1u << (q - 32u * k)) - 1u));
         }
-        if (pend == kNone && !cur) break;
-        // Deferred tile: LOD gathers by every thread, lookback by warp 0
-        // after it has published the current tile's aggregate.
-        uint32_t vis_bits = 0;
-        uint4 ent[kLeafChunk];
-        if (pend != kNone) {
-            vis_bits = tile_vis_bits(sm[p ^ 1]);
-            gather_rows<0>(a, stash[p ^ 1], vis_bits, ent);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            total += __shfl_xor_sync(~0u, total, o);
+            before += __shfl_xor_sync(~0u, before, o);
         }
-        if (warp == 0) {
-            if (cur && t == 0) LeafTile::publish(sm[p], s.tile_state, tile, 0, off, b, a.fault);
-            if (pend != kNone) LeafTile::resolve(sm[p ^ 1], s.tile_state, pend, 0, a.spin_limit_ns, a.error);
-        }
-        __syncthreads();
-        if (pend != kNone) {
-            const uint32_t pb = pend * (uint32_t)kLeafTile;
-            LeafTile::write_cmds<0, kLeafChunk>(sm[p ^ 1], vis_bits, ent, pb, off, a.cmds);
-            if constexpr (kLeafIpt > kLeafChunk) {
-                // The second chunk: rows [kLeafIpt - kLeafChunk, kLeafIpt).
-                constexpr int J0 = kLeafIpt - kLeafChunk;
-                gather_rows<J0>(a, stash[p ^ 1], vis_bits, ent);
-                LeafTile::write_cmds<J0, kLeafIpt>(sm[p ^ 1], vis_bits, ent, pb, off, a.cmds);
-            }
-            LeafTile::write_counts(sm[p ^ 1], pb, a.n, pend == 0, off, a.num_state_sets, a.counts);
-        }
-        if (!cur) break;
-        // The current tile becomes the deferred one.
-        if (t == 0) s_tile = atomicAdd(&s.ctl->tile_counter, 1u);
-        __syncthreads();
-        pend = tile;
-        tile = s_tile;
-        p ^= 1;
+        if (lane == 0) a.tile_words[tile] = head ? (total - before) | kTileHead : total;
     }
-    if (t == 0) finish_pass(s.ctl);
+}
+
+// Plain pass, launch 2 of 3, one CTA: replaces every tile word by the
+// tile's carry, the visible drawables of the region holding the tile's
+// first drawable that precede the tile.  A segmented exclusive scan in
+// chunks of 8 tiles per thread; a region start in a tile restarts the sum
+// at that tile's count.  It lets its dependent (the write kernel) launch
+// at once: that kernel reads the carries only after griddepcontrol.wait,
+// which returns when this grid has completed and its writes are visible.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 8;
+
+__global__ void __launch_bounds__(kScanThreads) leaf_tile_scan_kernel(uint32_t* __restrict__ words, uint32_t tiles)
+{
+    __shared__ uint32_t s_val[kScanThreads / kWarp], s_head[kScanThreads / kWarp];
+    __shared__ uint32_t s_run;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    grid_dependents_launch();
+    if (t == 0) s_run = 0;
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 < tiles; c0 += (uint32_t)(kScanThreads * kScanPer)) {
+        uint32_t w[kScanPer];
+        uint32_t v = 0, h = 0;  // this thread's segmented total and whether it holds a head
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            const uint32_t idx = c0 + (uint32_t)(t * kScanPer + k);
+            w[k] = idx < tiles ? words[idx] : 0u;
+            if (w[k] & kTileHead) {
+                v = w[k] & ~kTileHead;
+                h = 1;
+            } else {
+                v += w[k];
+            }
+        }
+        // Inclusive warp scan of (head, value) pairs: a later head resets.
+        uint32_t iv = v, ih = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t pv = __shfl_up_sync(~0u, iv, o), ph = __shfl_up_sync(~0u, ih, o);
+            if (lane >= o && !ih) {
+                iv += pv;
+                ih = ph;
+            }
+        }
+        if (lane == 31) {
+            s_val[warp] = iv;
+            s_head[warp] = ih;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t wv = s_val[lane], wh = s_head[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t pv = __shfl_up_sync(~0u, wv, o), ph = __shfl_up_sync(~0u, wh, o);
+                if (lane >= o && !wh) {
+                    wv += pv;
+                    wh = ph;
+                }
+            }
+            s_val[lane] = wv;  // inclusive over warps 0..lane
+            s_head[lane] = wh;
+        }
+        __syncthreads();
+        // Exclusive prefix of this thread: chunk carry-in, earlier warps, earlier lanes.
+        uint32_t ev = s_run, eh = 0;
+        if (warp > 0) {
+            const uint32_t pv = s_val[warp - 1], ph = s_head[warp - 1];
+            ev = ph ? pv : ev + pv;
+            eh = ph;
+        }
+        {
+            const uint32_t pv = __shfl_up_sync(~0u, iv, 1), ph = __shfl_up_sync(~0u, ih, 1);
+            if (lane > 0) {
+                ev = ph ? pv : ev + pv;
+                eh |= ph;
+            }
+        }
+        (void)eh;
+        uint32_t run = ev;
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            const uint32_t idx = c0 + (uint32_t)(t * kScanPer + k);
+            if (idx < tiles) words[idx] = run;
+            run = (w[k] & kTileHead) ? (w[k] & ~kTileHead) : run + w[k];
+        }
+        __syncthreads();
+        if (t == kScanThreads - 1) s_run = run;
+        __syncthreads();
+    }
+}
+
+constexpr uint32_t kWriteOffsetCap = 4096;  // StateSet offsets staged in shared memory
+#ifndef CADR_WRITE_CTAS_PER_SM
+#define CADR_WRITE_CTAS_PER_SM 6
+#endif
+
+// Plain pass, launch 3 of 3: one CTA per tile writes the commands and
+// counts from the planes and the tile's carry.  No CTA waits for another.
+// It is launched as a programmatic dependent of the tile scan: everything
+// but the carry (the planes, the geometry ids, the offsets, the LOD-table
+// gathers) is loaded while the scan still runs, and only the carry is read
+// after griddepcontrol.wait.  The loads are independent of one another,
+// so a tile costs about two memory round trips.
+__global__ void __launch_bounds__(kLeafThreads, CADR_WRITE_CTAS_PER_SM) leaf_write_kernel(const LeafArgs a)
+{
+    __shared__ LeafTile::Smem sm;
+    extern __shared__ uint32_t s_off[];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t tile = blockIdx.x, b = tile * (uint32_t)kLeafTile;
+    const uint32_t stride = (uint32_t)leaf_plane_stride(a.n);
+    const uint32_t* off = stage_offsets(s_off, a.off_cap, a.offsets, a.num_state_sets);
+    uint32_t vw[kLeafIpt], l0[kLeafIpt], l1[kLeafIpt], geo[kLeafIpt];
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
+        const uint32_t i = i0 + (uint32_t)lane;
+        vw[j] = i0 < a.n ? __ldg(a.planes + (i0 >> 5)) : 0u;
+        l0[j] = i0 < a.n ? __ldg(a.planes + stride + (i0 >> 5)) : 0u;
+        l1[j] = i0 < a.n ? __ldg(a.planes + 2 * stride + (i0 >> 5)) : 0u;
+        geo[j] = i < a.n ? __ldg(a.geometry + i) : 0u;
+    }
+    uint32_t vis_bits = 0, lod_bits = 0;
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        vis_bits |= ((vw[j] >> lane) & 1u) << j;
+        lod_bits |= (((l0[j] >> lane) & 1u) | (((l1[j] >> lane) & 1u) << 1)) << (2 * j);
+        if (lane == 0) sm.ballot[j][warp] = vw[j];
+    }
+    uint4 ent[kLeafIpt];
+    LeafTile::gather(vis_bits, lod_bits, geo, a.lods, a.num_geometries, a.num_lods, a.error, ent);
+    grid_dependency_wait();
+    if (t == 0) sm.info[2] = load_relaxed_u32(a.tile_words + tile);
+    __syncthreads();
+    LeafTile::scan(sm, off, a.num_state_sets, b, a.n);
+    LeafTile::write_ent(sm, vis_bits, ent, b, a.n, tile == 0, off, a.num_state_sets, a.cmds, a.counts);
 }
 
 // Internal level propagation.  With `staged`, the CTA's run of parents
@@ -333,40 +405,30 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-// StateSet offsets are staged in shared memory up to this many entries.
-constexpr uint32_t kLeafOffsetCap = 4096;
-constexpr size_t kLeafFixedSmem = 2 * sizeof(LeafStash) + kLeafThreads * 4 * sizeof(float4);
-constexpr size_t kLeafMaxSmem = kLeafFixedSmem + kLeafOffsetCap * sizeof(uint32_t);
-constexpr int kMaxDevices = 64;
-std::atomic<bool> g_leaf_attr_set[kMaxDevices];
-
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream)
 {
     if (a.n == 0) return cudaSuccess;
-    int dev = 0, sms = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    if (!g_leaf_attr_set[dev].load(std::memory_order_acquire)) {
-        e = cudaFuncSetAttribute(leaf_cull_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLeafMaxSmem);
-        if (e != cudaSuccess) return e;
-        g_leaf_attr_set[dev].store(true, std::memory_order_release);
-    }
-    LeafArgs b = a;
-    b.off_cap = kLeafOffsetCap;
-    const size_t smem = kLeafFixedSmem +
-                        ((a.num_state_sets + 1 <= kLeafOffsetCap) ? a.num_state_sets + 1 : 0) * sizeof(uint32_t);
-    // Persistent grid: the CTAs resident at once (at most kLeafCtasPerSm per
-    // SM by the launch bounds).  Any grid size is correct, since running
-    // CTAs take the tiles in order.
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, leaf_cull_kernel, kLeafThreads, smem);
-    if (e != cudaSuccess) return e;
     const uint32_t tiles = (a.n + kLeafTile - 1) / kLeafTile;
-    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms * (uint32_t)std::max(per_sm, 1));
-    leaf_cull_kernel<<<grid, kLeafThreads, smem, stream>>>(b, s);
-    return cudaGetLastError();
+    LeafArgs b = a;
+    b.planes = s.planes;
+    b.tile_words = reinterpret_cast<uint32_t*>(s.tile_state);
+    leaf_stream_kernel<<<tiles, kLeafThreads, 0, stream>>>(b);
+    leaf_tile_scan_kernel<<<1, kScanThreads, 0, stream>>>(b.tile_words, tiles);
+    LeafArgs c = b;
+    c.off_cap = kWriteOffsetCap;
+    const size_t smem = ((a.num_state_sets + 1 <= kWriteOffsetCap) ? a.num_state_sets + 1 : 0) * sizeof(uint32_t);
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(tiles);
+    cfg.blockDim = dim3(kLeafThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, leaf_write_kernel, c);
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 }  // namespace cadr

@@ -14,6 +14,8 @@ struct Scratch {
     uint64_t* tile_state = nullptr;
     uint64_t capacity = 0;      // tile states available
     uint64_t launches = 0;      // passes run since the last full reset
+    uint32_t* planes = nullptr; // plain pass: visibility and LOD bit-planes
+    uint64_t plane_words = 0;   // words available in `planes`
 };
 
 struct LeafArgs {
@@ -35,9 +37,9 @@ struct LeafArgs {
     uint32_t* counts;             // S
     uint32_t* marginal;           // ceil(N/32) or nullptr
     uint32_t* error;              // device-visible error word
-    uint64_t spin_limit_ns;
-    uint32_t fault;
     uint32_t off_cap;             // offsets staged in shared memory when S+1 <= off_cap (set by the launcher)
+    uint32_t* planes;             // 3 planes of leaf_plane_stride(N) words: visibility, LOD bits 0, 1 (set by the launcher)
+    uint32_t* tile_words;         // one word per leaf tile (set by the launcher)
     ViewConst view;
 };
 
@@ -61,10 +63,7 @@ struct ViewJob {
 };
 
 constexpr int kLeafThreads = 256;
-#ifndef CADR_LEAF_IPT
-#define CADR_LEAF_IPT 8
-#endif
-constexpr int kLeafIpt = CADR_LEAF_IPT;
+constexpr int kLeafIpt = 8;
 constexpr int kLeafTile = kLeafThreads * kLeafIpt;
 constexpr int kPropThreads = 256;
 
@@ -77,13 +76,19 @@ cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, c
 // Leaf level propagation (+ optional world spheres) without culling.
 cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 
-// Fused plain pass over the leaf level: propagate, transform spheres, cull,
-// select LOD, compact per StateSet.
+// Plain pass over the leaf level: propagate, transform spheres, cull,
+// select LOD, compact per StateSet.  Three launches on `stream`; needs
+// s.tile_state for ceil(n / kLeafTile) words and s.planes for
+// leaf_plane_words(n).
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream);
+constexpr uint32_t kLeafCullLaunches = 3;
+// Words of one bit-plane (one per 32 drawables), padded to 16 bytes.
+__host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 31) / 32 + 3) & ~uint64_t(3); }
+__host__ __device__ constexpr uint64_t leaf_plane_words(uint64_t n) { return 3 * leaf_plane_stride(n); }
 
 // Batched sphere cull: one persistent launch over all (view, tile) items.
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items,
-                                Scratch& s, uint32_t* error, uint64_t spin_limit_ns,
+                                Scratch& s, uint32_t* error, uint64_t spin_limit_ns, uint32_t fault,
                                 uint32_t block_threads, uint32_t items_per_thread, uint32_t grid,
                                 cudaStream_t stream);
 uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread);

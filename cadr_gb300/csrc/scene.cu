@@ -94,8 +94,6 @@ LeafArgs leaf_args(cadr_scene* sc)
     a.world = reinterpret_cast<float4*>(sc->buf.world);
     a.world_sphere = nullptr;
     a.error = sc->ctx->d_error;
-    a.spin_limit_ns = sc->ctx->spin_limit_ns;
-    a.fault = sc->ctx->fault;
     return a;
 }
 
@@ -287,6 +285,7 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     }
     const uint64_t tiles = (sc->desc.num_drawables + kLeafTile - 1) / kLeafTile;
     st = scratch_reserve(ctx, ctx->scratch, tiles);
+    if (st == CADR_OK) st = scratch_reserve_planes(ctx, ctx->scratch, leaf_plane_words(sc->desc.num_drawables));
     if (st != CADR_OK) return st;
     if (ctx->pass_recorded) {
         e = cudaStreamWaitEvent(s, ctx->pass_done, 0);
@@ -308,11 +307,11 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     a.view = to_view_const(*view);
     e = launch_leaf_cull(a, ctx->scratch, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull: launch");
+    ctx->launches += kLeafCullLaunches;
     if (fev) {
         cudaEventRecord(fev[2], s);
         ctx->frame_head++;
     }
-    ctx->launches++;
     ctx->scratch.launches++;
     e = cudaEventRecord(ctx->pass_done, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull: record");

@@ -208,7 +208,7 @@ static cadr_status launch_slot(cadr_server* srv, Slot* slot, std::vector<Request
     e = cudaMemcpyAsync(slot->d_jobs, slot->h_jobs, nv * sizeof(ViewJob), cudaMemcpyHostToDevice, slot->stream);
     if (e == cudaSuccess)
         e = launch_batched_cull(slot->d_jobs, nv, (uint32_t)total, slot->scratch, ctx->d_error, ctx->spin_limit_ns,
-                                tu.block_threads, tu.items_per_thread, grid, slot->stream);
+                                CADR_FAULT_NONE, tu.block_threads, tu.items_per_thread, grid, slot->stream);
     if (e != cudaSuccess) return cuda_fail(e, "server: launch");
     ctx->launches++;
     slot->scratch.launches++;

@@ -1,10 +1,10 @@
 // static_scratch.cu - the plain pass with its scratch memory in a statically
 // allocated device array, for callers that cannot allocate device memory.
 //
-// cadr_cull keeps its lookback scratch (the tile counter, the completion
-// counter and one status word per tile of 2,048 drawables) in memory it
-// allocates with cudaMalloc, and grows it, after a device-wide
-// synchronisation, when a scene needs more tiles than it holds.  Some
+// cadr_cull keeps its scratch (one word per tile of 2,048 drawables and
+// three bit-planes of one word per 32 drawables) in memory it allocates
+// with cudaMalloc, and grows it, after a device-wide synchronisation, when
+// a scene needs more than it holds.  Some
 // callers cannot let that happen: a renderer whose device memory is owned
 // and budgeted by the host application (every buffer imported or carved
 // out at start-up), or a frame loop that must not stall, since cudaMalloc
@@ -26,8 +26,9 @@ namespace {
 // Largest scene the entry point accepts, and the tiles it needs.
 constexpr uint64_t kStaticMaxDrawables = 33554432;
 constexpr uint64_t kStaticMaxTiles = (kStaticMaxDrawables + kLeafTile - 1) / kLeafTile;
-constexpr size_t kCtlBytes = 256;  // LookbackCtl, padded to keep the tile states 256-byte aligned
-constexpr size_t kStaticScratchBytes = kCtlBytes + kStaticMaxTiles * sizeof(uint64_t);  // 128 KiB + 256 B for 2,048-drawable tiles
+constexpr size_t kTileBytes = kStaticMaxTiles * sizeof(uint64_t);                       // 128 KiB
+constexpr size_t kPlaneBytes = leaf_plane_words(kStaticMaxDrawables) * sizeof(uint32_t);  // 12 MiB
+constexpr size_t kStaticScratchBytes = kTileBytes + kPlaneBytes;
 
 // The scratch.  Host code must not take this symbol's address directly: on
 // the host it names a stand-in, not device memory.  The device address comes
@@ -84,15 +85,13 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
         if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: clear counts");
         return CADR_OK;
     }
-    const uint64_t tiles = (sc->desc.num_drawables + kLeafTile - 1) / kLeafTile;
+    // Every word of the tile states and planes that a pass reads, the pass
+    // writes first: the array needs no clearing between calls.
     Scratch scratch;
-    scratch.ctl = static_cast<LookbackCtl*>(base);
-    scratch.tile_state = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(base) + kCtlBytes);
+    scratch.tile_state = static_cast<uint64_t*>(base);
     scratch.capacity = kStaticMaxTiles;
-    // The array keeps the previous call's contents: zero the control block
-    // and this pass's tile states (epoch 0, nothing published) first.
-    e = cudaMemsetAsync(base, 0, kCtlBytes + tiles * sizeof(uint64_t), s);
-    if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: clear scratch");
+    scratch.planes = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kTileBytes);
+    scratch.plane_words = leaf_plane_words(kStaticMaxDrawables);
     st = propagate_levels(sc, s);
     if (st != CADR_OK) return st;
     LeafArgs a = leaf_args(sc);
@@ -102,7 +101,7 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
     a.view = to_view_const(*view);
     e = launch_leaf_cull(a, scratch, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: launch");
-    ctx->launches++;
+    ctx->launches += kLeafCullLaunches;
     return CADR_OK;
 }
 

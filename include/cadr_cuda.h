@@ -258,17 +258,16 @@ CADR_API cadr_status cadr_cull(cadr_scene* scene, const cadr_view* view,
  * device memory while they run: a renderer whose device memory is owned and
  * budgeted by the host application, or a frame loop that cannot afford the
  * device-wide synchronisation of cudaMalloc/cudaFree, which cadr_cull may
- * perform when a scene needs more lookback scratch than it holds.  Same
+ * perform when a scene needs more scratch than it holds.  Same
  * kernels and bit-identical results as cadr_cull; the caller still passes
- * the outputs.  The scratch is a static device array of 128 KiB + 256 B
+ * the outputs.  The scratch is a static device array of 12 MiB + 128 KiB
  * (held by every GPU that loads the library until exit), which limits scenes
  * to 33,554,432 drawables; larger ones are rejected with
  * CADR_ERR_INVALID_ARG, as are scenes not committed yet.  The first call on
  * a device looks up the array's device address (set-up): make that first
- * call before any stream capture.  Every call shares the one array, which
- * keeps the last call's contents (each call clears what must start at
- * zero), so calls whose work overlaps on the GPU race: keep them on one
- * stream or otherwise ordered. */
+ * call before any stream capture.  Every call shares the one array, so
+ * calls whose work overlaps on the GPU race: keep them on one stream or
+ * otherwise ordered. */
 CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* scene, const cadr_view* view,
                                               cadr_draw_indexed_cmd* cmds, uint32_t* counts,
                                               uint32_t* marginal, cadr_stream stream);
@@ -324,9 +323,10 @@ CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_
 CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t* error_bits);
 
 /* Fault injection for the bounded-wait tests: while set, the first tile of
- * every plain pass never publishes its lookback status, so its successors'
- * waits run into the spin limit and cadr_context_check_device_error returns
- * CADR_ERR_TIMEOUT.  The pass still ends; the context stays usable. */
+ * every view of a batched pass (cadr_cull_batched) never publishes its
+ * lookback status, so its successors' waits run into the spin limit and
+ * cadr_context_check_device_error returns CADR_ERR_TIMEOUT.  The pass still
+ * ends; the context stays usable.  (The plain pass has no waits.) */
 #define CADR_FAULT_NONE 0u
 #define CADR_FAULT_SKIP_FIRST_TILE_PUBLISH 1u
 CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault);

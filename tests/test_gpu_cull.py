@@ -105,6 +105,16 @@ def test_c2_full_size_against_oracle(ctx):
     assert 0.2 <= frac <= 0.4
 
 
+def test_tile_scan_spans_chunks(ctx):
+    """More tiles than the tile scan takes in one chunk (8,192 tiles of
+    2,048 drawables), with three StateSets, so regions carry their counts
+    across the chunk boundary, and a ragged last tile."""
+    sc = scenes.config2(n=20_000_001, num_state_sets=3)
+    res, _, _ = gpu_cull(ctx, sc)
+    ref = bind.cull(sc, sc.views[0])
+    assert_same(res, ref, sc.state_set_offsets)
+
+
 def test_staged_upload_path_equals_pinned(ctx):
     """Host inputs from pageable memory go through the pinned ring on the
     side stream; from pinned memory they are copied directly: same result."""
