@@ -3,16 +3,19 @@
 Default workload: the plain pass on the large CAD scene (C2: 16,777,216
 drawables in 256 StateSets, hierarchy 4,096 -> 65,536 -> 1,048,576 ->
 drawables, 3 LODs, seed 1).  One step = one full pass: propagation of every
-hierarchy level, then the fused leaf kernel (world matrices, bounding
-spheres, frustum cull, LOD, per-StateSet compaction).
+hierarchy level, then the leaf stage (world matrices, bounding spheres,
+frustum cull, LOD, per-StateSet compaction) in three launches: the stream
+kernel, the tile scan and the write kernel.
 
   value  Gdrawables/s with the scene resident in HBM (inputs 1.6 GB > L2, so
          no L2 flush between steps is needed)
   e2e    same metric through the C ABI with host buffers: every step uploads
          all per-drawable inputs from pinned host memory, runs the pass and
          reads the per-StateSet counts and the visible commands back
-  roofline  the fused leaf kernel's algorithmic bytes per launch over its
-         average launch time (CUDA events on the launching stream)
+  roofline  the dominant kernel (the leaf stream kernel): its algorithmic
+         bytes per launch over its average launch time, CUDA events on the
+         launching stream; `leaf_stage` gives the same for the three leaf
+         launches together
 
 `--impl reference` times the CPU restatement of the pass (the oracle,
 OpenMP over all host cores) on the same workload: the reference itself has
@@ -73,13 +76,14 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """Per-launch DRAM traffic of the leaf kernel on the full C2 scene from
-    the committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", "leaf_cull_c2.md")
+def committed_traffic(key: str):
+    """Per-launch DRAM traffic on the full C2 scene from the committed ncu
+    summary of the leaf stage (`key`: stream_kernel_traffic_bytes or
+    leaf_stage_traffic_bytes), or None."""
+    p = os.path.join(ROOT, "profiles", "leaf_stage_c2.md")
     if not os.path.exists(p):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    m = re.search(key + r":\s*([0-9.eE+]+)", open(p).read())
     return float(m.group(1)) if m else None
 
 
@@ -134,13 +138,22 @@ class ClockSampler:
 
 
 def leaf_algorithmic_bytes(sc, visible: int) -> int:
-    """Compulsory DRAM bytes of one fused leaf launch: per drawable the local
+    """Compulsory DRAM bytes of the leaf stage: per drawable the local
     matrix (64), parent index (4), local sphere (16), geometry index (4) and
     world matrix written (64); per visible drawable its 20-byte command; the
-    marginal bitmask (N/8); every parent world matrix read once."""
+    marginal bitmask (N/8); every parent world matrix read once.  The
+    stage's own bit-planes and tile words are not counted."""
     n = sc.n
     parents = sc.level_sizes[-1] if sc.level_sizes else 0
     return n * (64 + 4 + 16 + 4 + 64) + 20 * visible + (n + 7) // 8 + 64 * parents
+
+
+def stream_algorithmic_bytes(sc) -> int:
+    """The stream kernel's share of leaf_algorithmic_bytes: everything but
+    the geometry indices and the commands, which the write kernel moves."""
+    n = sc.n
+    parents = sc.level_sizes[-1] if sc.level_sizes else 0
+    return n * (64 + 4 + 16 + 64) + (n + 7) // 8 + 64 * parents
 
 
 def step_algorithmic_bytes(sc, visible: int) -> int:
@@ -489,6 +502,7 @@ def main():
         ms = float(t.item())
     leaf_ms = float(np.mean([f[1] for f in frames])) if frames else None
     prop_ms = float(np.mean([f[0] for f in frames])) if frames else None
+    stream_ms = float(np.mean([f[3] for f in frames])) if frames else None
 
     # ---- end to end through the C ABI with host buffers -------------------
     e2e_steps = args.e2e_steps or min(args.steps, 50)
@@ -545,7 +559,9 @@ def main():
     value = world * sc.n / (ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     leaf_bytes = leaf_algorithmic_bytes(sc, visible)
-    achieved = leaf_bytes / (leaf_ms / 1e3) / 1e9 if leaf_ms else None
+    achieved_stage = leaf_bytes / (leaf_ms / 1e3) / 1e9 if leaf_ms else None
+    stream_bytes = stream_algorithmic_bytes(sc)
+    achieved = stream_bytes / (stream_ms / 1e3) / 1e9 if stream_ms else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -555,10 +571,16 @@ def main():
                    "visible_fraction": visible / sc.n, "l2": "inputs larger than L2 (no flush)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": committed_traffic(),
-                     "kernel": "leaf_kernel<true> (fused propagate+sphere+cull+LOD+compact)",
-                     "algorithmic_bytes_per_launch": leaf_bytes, "launch_ms": leaf_ms,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": committed_traffic("stream_kernel_traffic_bytes"),
+                     "kernel": "leaf_stream_kernel (world matrices, spheres, cull, LOD; bit-planes)",
+                     "algorithmic_bytes_per_launch": stream_bytes, "launch_ms": stream_ms,
                      "peak_source": f"{peak_kind} hbm_gbs"},
+        "leaf_stage": {"kernels": "leaf_stream_kernel + leaf_tile_scan_kernel + leaf_write_kernel",
+                       "achieved": achieved_stage, "unit": "GB/s",
+                       "frac": (achieved_stage / peak) if achieved_stage else None,
+                       "algorithmic_bytes": leaf_bytes, "ms": leaf_ms,
+                       "traffic": committed_traffic("leaf_stage_traffic_bytes")},
         "step": {"propagate_ms": prop_ms, "leaf_ms": leaf_ms,
                  "step_algorithmic_bytes": step_algorithmic_bytes(sc, visible),
                  "step_gbs": step_algorithmic_bytes(sc, visible) / (ms / 1e3) / 1e9},

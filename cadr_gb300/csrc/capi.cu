@@ -214,7 +214,7 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
     destroy_batched_state(ctx);
     scratch_release(ctx->scratch);
     for (int f = 0; f < cadr_context::kFrames; f++)
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < 4; k++)
             if (ctx->frame_ev[f][k]) cudaEventDestroy(ctx->frame_ev[f][k]);
     if (ctx->ring) cudaFreeHost(ctx->ring);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
@@ -270,7 +270,7 @@ CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int 
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "set_collect_frame_info: null context");
     if (on && !ctx->frame_ev[0][0]) {
         for (int f = 0; f < cadr_context::kFrames; f++)
-            for (int k = 0; k < 3; k++) {
+            for (int k = 0; k < 4; k++) {
                 cudaError_t e = cudaEventCreate(&ctx->frame_ev[f][k]);
                 if (e != cudaSuccess) return cuda_fail(e, "set_collect_frame_info: events");
             }
@@ -287,14 +287,14 @@ CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_
     uint32_t k = 0;
     while (k < max_frames && ctx->frame_tail < ctx->frame_head) {
         cudaEvent_t* ev = ctx->frame_ev[ctx->frame_tail % cadr_context::kFrames];
-        cudaError_t e = cudaEventSynchronize(ev[2]);
+        cudaError_t e = cudaEventSynchronize(ev[3]);
         if (e != cudaSuccess) return cuda_fail(e, "get_frame_infos: wait");
         cadr_frame_info& fi = out[k++];
         fi.frame = ctx->frame_tail;
         cudaEventElapsedTime(&fi.propagate_ms, ev[0], ev[1]);
-        cudaEventElapsedTime(&fi.leaf_ms, ev[1], ev[2]);
-        cudaEventElapsedTime(&fi.total_ms, ev[0], ev[2]);
-        fi.reserved = 0;
+        cudaEventElapsedTime(&fi.leaf_ms, ev[1], ev[3]);
+        cudaEventElapsedTime(&fi.total_ms, ev[0], ev[3]);
+        cudaEventElapsedTime(&fi.stream_ms, ev[1], ev[2]);
         ctx->frame_tail++;
     }
     *num_frames = k;

@@ -39,7 +39,7 @@ struct cadr_context {
     // frame timing ring (cadr_frame_info)
     static constexpr int kFrames = 256;
     bool collect_frames = false;
-    cudaEvent_t frame_ev[kFrames][3] = {};
+    cudaEvent_t frame_ev[kFrames][4] = {};  // before levels, after levels, after stream kernel, after leaf stage
     uint64_t frame_head = 0, frame_tail = 0;
 };
 

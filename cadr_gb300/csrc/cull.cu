@@ -405,7 +405,7 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream)
+cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream)
 {
     if (a.n == 0) return cudaSuccess;
     const uint32_t tiles = (a.n + kLeafTile - 1) / kLeafTile;
@@ -413,6 +413,10 @@ cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream)
     b.planes = s.planes;
     b.tile_words = reinterpret_cast<uint32_t*>(s.tile_state);
     leaf_stream_kernel<<<tiles, kLeafThreads, 0, stream>>>(b);
+    if (after_stream) {
+        const cudaError_t er = cudaEventRecord(after_stream, stream);
+        if (er != cudaSuccess) return er;
+    }
     leaf_tile_scan_kernel<<<1, kScanThreads, 0, stream>>>(b.tile_words, tiles);
     LeafArgs c = b;
     c.off_cap = kWriteOffsetCap;

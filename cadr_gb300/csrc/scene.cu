@@ -305,11 +305,11 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     a.counts = counts;
     a.marginal = marginal;
     a.view = to_view_const(*view);
-    e = launch_leaf_cull(a, ctx->scratch, s);
+    e = launch_leaf_cull(a, ctx->scratch, s, fev ? fev[2] : nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "cull: launch");
     ctx->launches += kLeafCullLaunches;
     if (fev) {
-        cudaEventRecord(fev[2], s);
+        cudaEventRecord(fev[3], s);
         ctx->frame_head++;
     }
     ctx->scratch.launches++;

@@ -63,7 +63,7 @@ class RequestResult(C.Structure):
 
 class FrameInfo(C.Structure):
     _fields_ = [("frame", u64), ("propagate_ms", C.c_float), ("leaf_ms", C.c_float), ("total_ms", C.c_float),
-                ("reserved", u32)]
+                ("stream_ms", C.c_float)]
 
 
 _SIGS = {
@@ -259,7 +259,7 @@ class Context:
         out = []
         while True:
             check(self.lib.cadr_context_get_frame_infos(self.handle, buf, 256, C.byref(n)))
-            out += [(buf[i].propagate_ms, buf[i].leaf_ms, buf[i].total_ms) for i in range(n.value)]
+            out += [(buf[i].propagate_ms, buf[i].leaf_ms, buf[i].total_ms, buf[i].stream_ms) for i in range(n.value)]
             if n.value < 256:
                 return out
 

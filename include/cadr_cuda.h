@@ -311,9 +311,9 @@ CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* tunin
 typedef struct cadr_frame_info {
     uint64_t frame;
     float propagate_ms;     /* internal hierarchy levels */
-    float leaf_ms;          /* fused leaf kernel (propagate, cull, LOD, compact) */
+    float leaf_ms;          /* leaf stage: stream, tile scan and write kernels */
     float total_ms;
-    uint32_t reserved;
+    float stream_ms;        /* the leaf stream kernel alone (part of leaf_ms) */
 } cadr_frame_info;
 CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int on);
 CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_info* out,
