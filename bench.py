@@ -270,9 +270,88 @@ def run_tier_a(ctx, n: int, steps: int, warmup: int, peak: float):
     same = bool(np.array_equal(ctx.download(ind, np.uint32, (n, 4)), ref_ind) and
                 np.array_equal(ctx.download(ptr, np.uint64, (n, 4)), ref_ptr))
     gbs = n * 148 / (ms / 1e3) / 1e9
-    return {"workload": f"{n} drawables, 4,096 geometries, {im.num_handles} handles (level {im.level} tables)",
-            "gdrawables_per_s": n / (ms / 1e3) / 1e9, "ms": ms, "algorithmic_bytes_per_drawable": 148,
-            "achieved_gbs": gbs, "frac_of_peak": gbs / peak, "bit_exact_vs_oracle": same}
+    out = {"workload": f"{n} drawables, 4,096 geometries, {im.num_handles} handles (level {im.level} tables)",
+           "gdrawables_per_s": n / (ms / 1e3) / 1e9, "ms": ms, "algorithmic_bytes_per_drawable": 148,
+           "achieved_gbs": gbs, "frac_of_peak": gbs / peak, "bit_exact_vs_oracle": same}
+    out["pack"] = run_pack(ctx, im, steps, warmup, peak)
+    return out
+
+
+def run_pack(ctx, im, steps: int, warmup: int, peak: float):
+    """The per-frame StateSet packing of the Tier A records.  The reference
+    (StateSet::recordToCommandBuffer) copies each StateSet's list into the
+    staging buffer on the host, one memcpy per StateSet, and uploads the
+    staging buffer: both timed here (single host thread, pinned staging).
+    Against it: the device-resident pack (cadr_pack_*), its full repack and
+    a frame whose dirty rows (1% of the drawables, host records) are
+    patched.  The packed array is checked against the oracle."""
+    import torch
+    from cadr_gb300 import lib, tier_a
+    from oracle import bind
+    n = im.drawables.shape[0]
+    dfs, ss, li, perm, starts = tier_a.slot_layout(im.state_set_counts, seed=13)
+    pool = np.ascontiguousarray(im.drawables[perm])
+    # Reference path: the lists (one per StateSet, in list order) memcpy'd
+    # into pinned staging at drawableCounter, then uploaded.
+    lists = [np.ascontiguousarray(im.drawables[int(starts[j]):int(starts[j + 1])]) for j in range(len(dfs))]
+    staging = lib.PinnedBuffer(n * 48)
+    st_view = staging.view(tier_a.DRAWABLE_DTYPE, (n,))
+    dev = ctx.alloc(n * 48)
+    host_ms, h2d_ms = [], []
+    for rep in range(max(3, warmup)):
+        t0 = time.perf_counter()
+        counter = 0
+        for lst in lists:
+            st_view[counter:counter + len(lst)] = lst
+            counter += len(lst)
+        t1 = time.perf_counter()
+        ctx.upload(dev, st_view)
+        ctx.sync()
+        t2 = time.perf_counter()
+        host_ms.append((t1 - t0) * 1e3)
+        h2d_ms.append((t2 - t1) * 1e3)
+    pk = lib.Pack(ctx, n)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(pool)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(warmup):
+        pk.repack()
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(steps):
+        pk.repack()
+    e1.record(stream)
+    ctx.sync()
+    repack_ms = e0.elapsed_time(e1) / steps
+    packed, offsets = pk.fetch(tier_a.DRAWABLE_DTYPE)
+    ref, ref_off = bind.pack_state_sets(dfs, ss, li, pool)
+    same = bool(np.array_equal(packed.view(np.uint8), ref.view(np.uint8)) and np.array_equal(offsets, ref_off))
+    rs = np.random.default_rng(14)
+    dirty = rs.choice(n, size=n // 100, replace=False).astype(np.uint32)
+    d_rec = lib.PinnedBuffer(len(dirty) * 48)
+    d_slots = lib.PinnedBuffer(len(dirty) * 4)
+    d_rec.view(tier_a.DRAWABLE_DTYPE, (len(dirty),))[...] = pool[dirty]
+    d_slots.view(np.uint32, (len(dirty),))[...] = dirty
+    for _ in range(warmup):
+        lib.check(ctx.lib.cadr_pack_patch(pk.handle, d_slots.ptr, d_rec.ptr, len(dirty), None))
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(steps):
+        lib.check(ctx.lib.cadr_pack_patch(pk.handle, d_slots.ptr, d_rec.ptr, len(dirty), None))
+    e1.record(stream)
+    ctx.sync()
+    patch_ms = e0.elapsed_time(e1) / steps
+    ctx.check_device_error()
+    pk.close()
+    repack_gbs = n * (48 + 48 + 4) / (repack_ms / 1e3) / 1e9
+    return {"workload": f"{n} records of 48 B in {len(dfs)} StateSets, slots in random order",
+            "reference_host_pack_ms": float(np.median(host_ms)),
+            "reference_upload_ms": float(np.median(h2d_ms)),
+            "device_repack_ms": repack_ms, "device_repack_gbs": repack_gbs,
+            "device_repack_frac_of_peak": repack_gbs / peak,
+            "patch_1pct_ms": patch_ms, "patch_rows": int(len(dirty)),
+            "bit_exact_vs_oracle": same}
 
 
 def run_serving(args):

@@ -20,6 +20,7 @@ MAX_LEVELS = 16
 STATUS = {0: "CADR_OK", 1: "CADR_ERR_INVALID_ARG", 2: "CADR_ERR_OUT_OF_MEMORY", 3: "CADR_ERR_TIMEOUT",
           4: "CADR_ERR_CUDA", 5: "CADR_ERR_DEVICE", 6: "CADR_ERR_NOT_READY", 7: "CADR_ERR_REJECTED"}
 OK, INVALID_ARG, OUT_OF_MEMORY, TIMEOUT, CUDA, DEVICE, NOT_READY, REJECTED = range(8)
+DEVERR_LOOKBACK_TIMEOUT, DEVERR_MBARRIER_TIMEOUT, DEVERR_BAD_INDEX = 0x1, 0x2, 0x4
 FAULT_NONE, FAULT_SKIP_FIRST_TILE_PUBLISH = 0, 1
 
 # Exported symbols of the C ABI (checked against include/cadr_cuda.h by the tests).
@@ -105,6 +106,13 @@ _SIGS = {
                                C.POINTER(C.c_float)], i32),
     "cadr_get_tuning": ([vp, C.POINTER(Tuning)], i32),
     "cadr_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+    "cadr_pack_create": ([vp, u32, C.POINTER(vp)], i32),
+    "cadr_pack_destroy": ([vp], i32),
+    "cadr_pack_set_layout": ([vp, u32, u32, vp, vp, vp, vp], i32),
+    "cadr_pack_upload": ([vp, vp, u32, u32, vp], i32),
+    "cadr_pack_repack": ([vp, vp], i32),
+    "cadr_pack_patch": ([vp, vp, vp, u32, vp], i32),
+    "cadr_pack_buffers": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(u32)], i32),
     "cadr_server_create": ([vp, C.POINTER(ServerConfig), C.POINTER(vp)], i32),
     "cadr_server_destroy": ([vp], i32),
     "cadr_server_submit": ([vp, vp, vp, u32, C.POINTER(u64)], i32),
@@ -399,6 +407,61 @@ def autotune_batched(ctx: Context, arr, reps: int = 5):
     ms = C.c_float()
     check(ctx.lib.cadr_autotune_batched(ctx.handle, arr, len(arr), reps, C.byref(t), C.byref(ms)))
     return t, ms.value
+
+
+class Pack:
+    """Device-resident StateSet packing of Tier A records (cadr_pack_*)."""
+
+    def __init__(self, ctx: Context, capacity: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = vp()
+        check(self.lib.cadr_pack_create(ctx.handle, capacity, C.byref(h)))
+        self.handle = h.value
+
+    def set_layout(self, dfs_order, state_set_of_slot, list_index_of_slot, stream=None):
+        dfs = np.ascontiguousarray(dfs_order, np.uint32)
+        ss = np.ascontiguousarray(state_set_of_slot, np.uint32)
+        li = np.ascontiguousarray(list_index_of_slot, np.uint32)
+        check(self.lib.cadr_pack_set_layout(self.handle, len(ss), len(dfs), _ptr(dfs), _ptr(ss), _ptr(li), stream))
+        self.num_state_sets = len(dfs)
+
+    def upload(self, records: np.ndarray, first: int = 0, stream=None):
+        r = np.ascontiguousarray(records)
+        assert r.dtype.itemsize == 48
+        check(self.lib.cadr_pack_upload(self.handle, _ptr(r), first, len(r), stream))
+
+    def repack(self, stream=None):
+        check(self.lib.cadr_pack_repack(self.handle, stream))
+
+    def patch(self, slots, records: np.ndarray, stream=None):
+        sl = np.ascontiguousarray(slots, np.uint32)
+        r = np.ascontiguousarray(records)
+        assert r.dtype.itemsize == 48 and len(r) == len(sl)
+        check(self.lib.cadr_pack_patch(self.handle, _ptr(sl), _ptr(r), len(sl), stream))
+
+    def buffers(self):
+        packed, offsets, n = vp(), vp(), u32()
+        check(self.lib.cadr_pack_buffers(self.handle, C.byref(packed), C.byref(offsets), C.byref(n)))
+        return packed.value, offsets.value, n.value
+
+    def fetch(self, dtype):
+        """(packed records as `dtype`, region offsets) after a device sync."""
+        packed, offsets, n = self.buffers()
+        self.ctx.sync()
+        return (self.ctx.download(packed, dtype, (n,)),
+                self.ctx.download(offsets, np.uint32, (self.num_state_sets + 1,)))
+
+    def close(self):
+        if self.handle:
+            self.lib.cadr_pack_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

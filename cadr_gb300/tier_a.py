@@ -153,3 +153,22 @@ def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries:
     d = d[order]
     counts = np.bincount(ss, minlength=num_state_sets).astype(np.uint32)
     return TierAImage(img, base, level, int(root), np.ascontiguousarray(d), counts, H)
+
+
+def slot_layout(counts, seed: int):
+    """A slot layout (the input of the device-resident StateSet packing)
+    whose packing is a given grouping: region j of the packed array
+    (counts[j] records) belongs to StateSet dfs[j], and slot k holds the
+    record of packed position perm[k], a seeded random permutation.
+    Returns (dfs, state_set_of_slot, list_index_of_slot, perm, region
+    starts)."""
+    counts = np.asarray(counts, np.int64)
+    S, n = len(counts), int(counts.sum())
+    rs = np.random.default_rng(seed)
+    dfs = rs.permutation(S).astype(np.uint32)
+    starts = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    region_of_pos = np.repeat(np.arange(S), counts)
+    perm = rs.permutation(n)
+    set_of_slot = dfs[region_of_pos[perm]].astype(np.uint32)
+    list_index = (perm - starts[region_of_pos[perm]]).astype(np.uint32)
+    return dfs, set_of_slot, list_index, perm, starts.astype(np.uint32)

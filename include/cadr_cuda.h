@@ -215,6 +215,49 @@ CADR_API cadr_status cadr_process_drawables(cadr_context* ctx, uint32_t handle_l
                                             cadr_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* Device-resident StateSet packing of the Tier A records.  Replaces the
+ * per-frame host packing of StateSet::prepareRecording and
+ * StateSet::recordToCommandBuffer (src/CadR/StateSet.cpp:180-268), which
+ * copies every StateSet's DrawableGpuData list, in list order and in
+ * depth-first StateSet order, into the staging buffer at drawableCounter,
+ * and the upload of that buffer (Renderer.cpp:635-644).  The records stay
+ * in a device pool indexed by slot.  A layout gives every slot its
+ * StateSet and its index in that StateSet's list, and the StateSets in
+ * depth-first order; the device derives the regions and the packed
+ * position of every slot.  cadr_pack_repack builds the packed array that
+ * cadr_process_drawables reads; a frame whose records changed patches only
+ * those rows (cadr_pack_patch) in the pool and the packed array.  Every
+ * call is ordered on `stream`. */
+typedef struct cadr_pack cadr_pack;
+CADR_API cadr_status cadr_pack_create(cadr_context* ctx, uint32_t capacity, cadr_pack** out);
+CADR_API cadr_status cadr_pack_destroy(cadr_pack* pack);
+/* dfs_order[j]: the StateSet drawn j-th (a permutation of 0..num_state_sets-1);
+ * state_set_of_slot[k] and list_index_of_slot[k] for the slots
+ * 0..num_slots-1, the list indices of each StateSet being 0..n-1 once each.
+ * A layout that breaks these rules sets CADR_DEVERR_BAD_INDEX
+ * (cadr_context_check_device_error). */
+CADR_API cadr_status cadr_pack_set_layout(cadr_pack* pack, uint32_t num_slots, uint32_t num_state_sets,
+                                          const uint32_t* dfs_order, const uint32_t* state_set_of_slot,
+                                          const uint32_t* list_index_of_slot, cadr_stream stream);
+/* Records of the slots [first, first + count) from host memory, into the
+ * pool; the packed array follows at the next cadr_pack_repack. */
+CADR_API cadr_status cadr_pack_upload(cadr_pack* pack, const cadr_drawable_gpu_data* records, uint32_t first,
+                                      uint32_t count, cadr_stream stream);
+/* packed[p] = pool[slot at packed position p] for the whole layout. */
+CADR_API cadr_status cadr_pack_repack(cadr_pack* pack, cadr_stream stream);
+/* records[k] replaces slot slots[k], in the pool and in the packed array. */
+CADR_API cadr_status cadr_pack_patch(cadr_pack* pack, const uint32_t* slots, const cadr_drawable_gpu_data* records,
+                                     uint32_t count, cadr_stream stream);
+/* Device pointers: the packed records (num_slots of them) and the region
+ * offsets (num_state_sets + 1): StateSet dfs_order[j] occupies packed
+ * records [offsets[j], offsets[j+1]), which is the reference's
+ * drawableCounter at that StateSet; its draw is
+ * cmdDrawIndirect(offset = offsets[j] * 16, count = offsets[j+1] - offsets[j])
+ * over cadr_process_drawables' output. */
+CADR_API cadr_status cadr_pack_buffers(cadr_pack* pack, const cadr_drawable_gpu_data** packed,
+                                       const uint32_t** region_offsets, uint32_t* num_slots);
+
+/* ------------------------------------------------------------------------ */
 /* Tier B scenes. */
 CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc* desc,
                                        cadr_scene** out);

@@ -46,6 +46,8 @@ class OracleLib:
         L.oracle_cull_spheres.argtypes = [u64, vp, vp, u32, vp, u32, u32, vp, vp, vp, vp, vp, i32]
         L.oracle_cull_spheres.restype = i32
         L.oracle_max_threads.restype = i32
+        L.oracle_pack_state_sets.argtypes = [u32, vp, u64, vp, vp, vp, vp, vp]
+        L.oracle_pack_state_sets.restype = i32
 
 
 def load() -> OracleLib:
@@ -153,6 +155,23 @@ def process_drawables(image: np.ndarray, image_base: int, handle_level: int, roo
     if rc != 0:
         raise ValueError("oracle_process_drawables: a lookup left the memory image")
     return ind, ptr
+
+
+def pack_state_sets(dfs_order, state_set_of_slot, list_index_of_slot, pool):
+    """StateSet packing of the records `pool` (one per slot; any 48-byte
+    record dtype).  Returns (packed records, region offsets [S + 1])."""
+    L = load().lib
+    dfs = np.ascontiguousarray(dfs_order, np.uint32)
+    ss = np.ascontiguousarray(state_set_of_slot, np.uint32)
+    li = np.ascontiguousarray(list_index_of_slot, np.uint32)
+    pool = np.ascontiguousarray(pool)
+    assert pool.dtype.itemsize == 48
+    packed = np.zeros_like(pool)
+    offsets = np.zeros(len(dfs) + 1, np.uint32)
+    rc = L.oracle_pack_state_sets(len(dfs), _p(dfs), len(ss), _p(ss), _p(li), _p(pool), _p(packed), _p(offsets))
+    if rc != 0:
+        raise ValueError("oracle_pack_state_sets: the layout is not a set of lists")
+    return packed, offsets
 
 
 def valid_cmds(cmds: np.ndarray, counts: np.ndarray, offsets: np.ndarray) -> np.ndarray:

@@ -373,3 +373,74 @@ int oracle_cull(uint32_t num_levels, const uint64_t* level_size, const float* co
     if (!world_sphere) free(ws);
     return rc;
 }
+
+/* StateSet::prepareRecording counts each StateSet's drawables
+ * (StateSet.cpp:180-195); recordToCommandBuffer then copies each list at
+ * drawableCounter and advances it, StateSet by StateSet in depth-first
+ * order (StateSet.cpp:198-268).  The lists are rebuilt here from the
+ * (StateSet, list index) of every slot. */
+int oracle_pack_state_sets(uint32_t S, const uint32_t* dfs_order, uint64_t n, const uint32_t* state_set_of_slot,
+                           const uint32_t* list_index_of_slot, const cadr_drawable_gpu_data* pool,
+                           cadr_drawable_gpu_data* packed, uint32_t* offsets)
+{
+    int rc = 0;
+    uint64_t* count = (uint64_t*)calloc(S ? S : 1, sizeof(uint64_t));
+    uint64_t* first = (uint64_t*)calloc(S ? S : 1, sizeof(uint64_t));
+    uint8_t* seen_set = (uint8_t*)calloc(S ? S : 1, 1);
+    uint64_t* list = (uint64_t*)malloc((n ? n : 1) * sizeof(uint64_t));
+    uint8_t* used = (uint8_t*)calloc(n ? n : 1, 1);
+    if (!count || !first || !seen_set || !list || !used) {
+        rc = -1;
+        goto done;
+    }
+    for (uint32_t j = 0; j < S; j++) {
+        if (dfs_order[j] >= S || seen_set[dfs_order[j]]) {
+            rc = -1;
+            goto done;
+        }
+        seen_set[dfs_order[j]] = 1;
+    }
+    for (uint64_t k = 0; k < n; k++) {
+        if (state_set_of_slot[k] >= S) {
+            rc = -1;
+            goto done;
+        }
+        count[state_set_of_slot[k]]++;
+    }
+    /* the lists, StateSet after StateSet in id order */
+    {
+        uint64_t run = 0;
+        for (uint32_t s = 0; s < S; s++) {
+            first[s] = run;
+            run += count[s];
+        }
+    }
+    for (uint64_t k = 0; k < n; k++) {
+        const uint32_t s = state_set_of_slot[k];
+        const uint64_t li = list_index_of_slot[k];
+        if (li >= count[s] || used[first[s] + li]) {
+            rc = -1;
+            goto done;
+        }
+        used[first[s] + li] = 1;
+        list[first[s] + li] = k;
+    }
+    /* recordToCommandBuffer: drawableCounter over the depth-first order */
+    {
+        uint64_t drawable_counter = 0;
+        for (uint32_t j = 0; j < S; j++) {
+            const uint32_t s = dfs_order[j];
+            offsets[j] = (uint32_t)drawable_counter;
+            for (uint64_t li = 0; li < count[s]; li++) packed[drawable_counter + li] = pool[list[first[s] + li]];
+            drawable_counter += count[s];
+        }
+        offsets[S] = (uint32_t)drawable_counter;
+    }
+done:
+    free(count);
+    free(first);
+    free(seen_set);
+    free(list);
+    free(used);
+    return rc;
+}

@@ -50,6 +50,18 @@ int oracle_process_drawables_regions(const oracle_region* regions, uint32_t num_
                                      cadr_draw_indirect_cmd* indirect,
                                      cadr_drawable_pointers* pointers, int threads);
 
+/* StateSet packing of StateSet::prepareRecording / recordToCommandBuffer
+ * (src/CadR/StateSet.cpp:180-268): the StateSets are visited in
+ * depth-first order dfs_order[0..S-1]; each copies its drawable list (its
+ * slots, in list-index order) to packed[] at the running drawableCounter,
+ * which then advances by the list's length.  offsets[j] receives the
+ * counter at StateSet dfs_order[j], offsets[S] the total.  Returns -1 for a
+ * layout that is not a set of lists (a StateSet or list index out of range,
+ * a list index used twice, dfs_order not a permutation). */
+int oracle_pack_state_sets(uint32_t S, const uint32_t* dfs_order, uint64_t n, const uint32_t* state_set_of_slot,
+                           const uint32_t* list_index_of_slot, const cadr_drawable_gpu_data* pool,
+                           cadr_drawable_gpu_data* packed, uint32_t* offsets);
+
 /* GLM-order 4x4 product out = a * b (column-major float[16]). */
 void oracle_mat4_mul(const float* a, const float* b, float* out);
 /* BoundingSphere operator*: out = m * (cx, cy, cz, r). */

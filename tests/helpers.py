@@ -39,3 +39,10 @@ def scene_from_npz(g):
     return scenes.Scene("small", 11, [g["level0_local"], g["level1_local"]], [None, g["level1_parent"]],
                         g["local"], g["parent"], g["sphere"], g["geometry"], g["offsets"], lods,
                         int(g["num_lods"][0]), [view])
+
+
+
+def pack_layout_from_packed(counts, seed):
+    """tier_a.slot_layout: a slot layout whose packing is a given grouping."""
+    from cadr_gb300 import tier_a
+    return tier_a.slot_layout(counts, seed)

@@ -1,0 +1,142 @@
+"""Device-resident StateSet packing (cadr_pack_*) against the oracle's
+restatement of StateSet::recordToCommandBuffer, bit for bit, and Tier A
+run end to end on the packed array."""
+import numpy as np
+import pytest
+
+from cadr_gb300 import lib, tier_a
+from helpers import pack_layout_from_packed
+from oracle import bind
+
+pytestmark = pytest.mark.gpu
+
+
+def random_records(n, seed):
+    raw = np.random.default_rng(seed).integers(0, 2**63, size=(n, 6), dtype=np.uint64)
+    return raw.view(tier_a.DRAWABLE_DTYPE).reshape(n)
+
+
+def make_counts(S, n, seed, empty=()):
+    rs = np.random.default_rng(seed)
+    w = rs.random(S) + 0.05
+    for e in empty:
+        w[e] = 0.0
+    counts = np.floor(w / w.sum() * n).astype(np.int64)
+    counts[int(np.argmax(w))] += n - counts.sum()
+    return counts
+
+
+@pytest.mark.parametrize("n,S,empty", [(1, 1, ()), (1000, 7, (2, 6)), (100_003, 300, (0, 17, 299)),
+                                       (2_000_000, 64, (5,))])
+def test_repack_matches_oracle(ctx, n, S, empty):
+    counts = make_counts(S, n, n + S, empty)
+    dfs, ss, li, perm, starts = pack_layout_from_packed(counts, seed=n)
+    expect = random_records(n, seed=S)
+    pool = np.empty_like(expect)
+    pool[np.arange(n)] = expect[perm]
+    ref, ref_off = bind.pack_state_sets(dfs, ss, li, pool)
+    assert np.array_equal(ref.view(np.uint8), expect.view(np.uint8))
+    assert np.array_equal(ref_off, starts)
+    pk = lib.Pack(ctx, n)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(pool)
+    pk.repack()
+    packed, offsets = pk.fetch(tier_a.DRAWABLE_DTYPE)
+    assert ctx.check_device_error() == 0
+    assert np.array_equal(packed.view(np.uint8), ref.view(np.uint8))
+    assert np.array_equal(offsets, ref_off)
+
+
+def test_patch_dirty_rows(ctx):
+    n, S = 200_000, 40
+    counts = make_counts(S, n, 3)
+    dfs, ss, li, perm, _ = pack_layout_from_packed(counts, seed=4)
+    pool = random_records(n, seed=5)
+    pk = lib.Pack(ctx, n)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(pool)
+    pk.repack()
+    rs = np.random.default_rng(6)
+    for rnd in range(3):
+        dirty = rs.choice(n, size=n // 100, replace=False).astype(np.uint32)
+        new = random_records(len(dirty), seed=100 + rnd)
+        pool[dirty] = new
+        pk.patch(dirty, new)
+        ref, _ = bind.pack_state_sets(dfs, ss, li, pool)
+        packed, _ = pk.fetch(tier_a.DRAWABLE_DTYPE)
+        assert np.array_equal(packed.view(np.uint8), ref.view(np.uint8))
+    # The pool took the patches too: a full repack gives the same array.
+    pk.repack()
+    packed2, _ = pk.fetch(tier_a.DRAWABLE_DTYPE)
+    assert np.array_equal(packed2.view(np.uint8), ref.view(np.uint8))
+    assert ctx.check_device_error() == 0
+
+
+def test_relayout_moves_drawables(ctx):
+    """A new layout (drawables moved between StateSets, lists reordered)
+    over the same pool repacks to the oracle's packing of that layout."""
+    n, S = 50_000, 12
+    pool = random_records(n, seed=8)
+    pk = lib.Pack(ctx, n)
+    for seed in (9, 10):
+        dfs, ss, li, _, _ = pack_layout_from_packed(make_counts(S, n, seed, (seed % S,)), seed=seed)
+        pk.set_layout(dfs, ss, li)
+        if seed == 9:
+            pk.upload(pool)
+        pk.repack()
+        ref, ref_off = bind.pack_state_sets(dfs, ss, li, pool)
+        packed, offsets = pk.fetch(tier_a.DRAWABLE_DTYPE)
+        assert np.array_equal(packed.view(np.uint8), ref.view(np.uint8))
+        assert np.array_equal(offsets, ref_off)
+    assert ctx.check_device_error() == 0
+
+
+@pytest.mark.parametrize("case", ["duplicate index", "index past list", "set out of range", "dfs not a permutation"])
+def test_bad_layouts_are_reported(ctx, case):
+    n, S = 1000, 5
+    dfs, ss, li, _, _ = pack_layout_from_packed(make_counts(S, n, 1), seed=2)
+    dfs, ss, li = dfs.copy(), ss.copy(), li.copy()
+    if case == "duplicate index":
+        k = int(np.nonzero(li == 1)[0][0])
+        li[k] = 0
+    elif case == "index past list":
+        li[0] = n
+    elif case == "set out of range":
+        ss[0] = S
+    else:
+        dfs[1] = dfs[0]
+    pk = lib.Pack(ctx, n)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(random_records(n, seed=3))
+    pk.repack()
+    st, bits = ctx.device_error_status()
+    assert st == lib.DEVICE and bits & lib.DEVERR_BAD_INDEX
+
+
+def test_tier_a_on_packed_records(ctx):
+    """Records scattered over slots, packed on the device, then
+    processDrawables: the output equals the oracle on the reference's
+    host-packed records, so the draws address the same data."""
+    kw = dict(n=300_000, num_state_sets=24, num_geometries=4096, prims_per_geometry=3)
+    probe = tier_a.build(seed=11, base=1 << 40, **kw)
+    buf = ctx.alloc(probe.image.nbytes + 4096)
+    im = tier_a.build(seed=11, base=buf.ptr, **kw)
+    r_ind, r_ptr = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables)
+    ctx.upload(buf, im.image)
+    n = im.drawables.shape[0]
+    dfs, ss, li, perm, starts = pack_layout_from_packed(im.state_set_counts, seed=12)
+    pool = im.drawables[perm]
+    pk = lib.Pack(ctx, n)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(pool)
+    pk.repack()
+    packed, offsets, m = pk.buffers()
+    assert m == n
+    ind = ctx.alloc(n * 16)
+    ptr = ctx.alloc(n * 32)
+    ctx.process_drawables(im.level, im.root, packed, n, ind, ptr)
+    ctx.sync()
+    assert ctx.check_device_error() == 0
+    assert np.array_equal(ctx.download(ind, np.uint32, (n, 4)), r_ind)
+    assert np.array_equal(ctx.download(ptr, np.uint64, (n, 4)), r_ptr)
+    assert np.array_equal(ctx.download(offsets, np.uint32, (len(dfs) + 1,)), starts)

@@ -275,3 +275,77 @@ def test_view_record_layout():
     # inward normals: the camera-space point (0,0,-10) is inside every plane
     for p in v["planes"][0]:
         assert p[2] * -10.0 + p[3] >= 0
+
+
+class _StateSet:
+    """The reference StateSet as far as packing goes: a drawable list
+    (appended on creation, swap-removed on deletion) and child StateSets."""
+
+    def __init__(self):
+        self.drawables = []
+        self.children = []
+
+
+def _record_to_command_buffer(ss, out, regions, counter):
+    """StateSet::recordToCommandBuffer (StateSet.cpp:198-268): this
+    StateSet's list at drawableCounter, then the children depth-first."""
+    regions.append((ss, counter))
+    n = len(ss.drawables)
+    if n:
+        out[counter:counter + n] = ss.drawables
+        counter += n
+    for c in ss.children:
+        counter = _record_to_command_buffer(c, out, regions, counter)
+    return counter
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_pack_state_sets_matches_recursive_recording(seed):
+    """The oracle's packing equals the reference's recursive recording over
+    a random StateSet tree whose lists were built by appends and
+    swap-removes (so list order is not creation order)."""
+    from oracle import bind
+    rs = np.random.default_rng(seed)
+    S = int(rs.integers(1, 40))
+    sets = [_StateSet() for _ in range(S)]
+    for i in range(1, S):
+        sets[int(rs.integers(0, i))].children.append(sets[i])
+    live = {}
+    for rec in range(int(rs.integers(0, 3000))):
+        s = int(rs.integers(0, S))
+        if rs.random() < 0.3 and sets[s].drawables:
+            lst = sets[s].drawables
+            j = int(rs.integers(0, len(lst)))
+            lst[j] = lst[-1]
+            lst.pop()
+        else:
+            sets[s].drawables.append(rec)
+    slots = [(s, li, rec) for s in range(S) for li, rec in enumerate(sets[s].drawables)]
+    rs.shuffle(slots)
+    n = len(slots)
+    pool = np.zeros(n, tier_a.DRAWABLE_DTYPE)
+    pool["vertex_data_handle"] = [rec for _, _, rec in slots]
+    pool["primitive_set_offset"] = [li for _, li, _ in slots]
+    # Depth-first order of the tree and the expected packing.
+    expect_ids = np.zeros(n, np.int64)
+    regions = []
+    total = _record_to_command_buffer(sets[0], expect_ids, regions, 0)
+    assert total == n
+    index = {id(ss): k for k, ss in enumerate(sets)}
+    dfs = np.array([index[id(ss)] for ss, _ in regions], np.uint32)
+    packed, offsets = bind.pack_state_sets(dfs, [s for s, _, _ in slots], [li for _, li, _ in slots], pool)
+    assert np.array_equal(packed["vertex_data_handle"], expect_ids.astype(np.uint64))
+    assert offsets[:-1].tolist() == [c for _, c in regions] and offsets[-1] == n
+
+
+def test_pack_state_sets_rejects_bad_layouts():
+    from oracle import bind
+    pool = np.zeros(3, tier_a.DRAWABLE_DTYPE)
+    with pytest.raises(ValueError):
+        bind.pack_state_sets([0, 1], [0, 0, 1], [0, 0, 0], pool)   # list index used twice
+    with pytest.raises(ValueError):
+        bind.pack_state_sets([0, 1], [0, 0, 2], [0, 1, 0], pool)   # StateSet out of range
+    with pytest.raises(ValueError):
+        bind.pack_state_sets([0, 0], [0, 0, 1], [0, 1, 0], pool)   # not a permutation
+    with pytest.raises(ValueError):
+        bind.pack_state_sets([0, 1], [0, 0, 1], [0, 2, 0], pool)   # index past the list
