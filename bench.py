@@ -274,7 +274,52 @@ def run_tier_a(ctx, n: int, steps: int, warmup: int, peak: float):
            "gdrawables_per_s": n / (ms / 1e3) / 1e9, "ms": ms, "algorithmic_bytes_per_drawable": 148,
            "achieved_gbs": gbs, "frac_of_peak": gbs / peak, "bit_exact_vs_oracle": same}
     out["pack"] = run_pack(ctx, im, steps, warmup, peak)
+    out["consumer_check"] = run_consumer_check(ctx, steps=max(3, min(steps, 10)), warmup=2)
     return out
+
+
+def run_consumer_check(ctx, steps: int, warmup: int, n: int = 262_144):
+    """The vertex-pulling consumer check (cadr_check_draws) over the Tier A
+    draws of an image with index, vertex and matrix data (64 geometries of
+    1,024 vertices, 36..3,000 indices per PrimitiveSet): every vertex of
+    every draw pulled and transformed as the consumer vertex shader would.
+    Checked against the oracle on the first 4,096 draws."""
+    import torch
+    from cadr_gb300 import lib, tier_a
+    from oracle import bind
+    kw = dict(n=n, num_state_sets=8, num_geometries=64, prims_per_geometry=3, geometry_data=True)
+    dev = ctx.alloc(tier_a.image_size(**{k: v for k, v in kw.items() if k != "num_state_sets"}) + 4096)
+    im = tier_a.build(seed=31, base=dev.ptr, **kw)
+    ctx.upload(dev, im.image)
+    d = ctx.to_device(im.drawables)
+    ind, ptr, out = ctx.alloc(n * 16), ctx.alloc(n * 32), ctx.alloc(n * 16)
+    ctx.process_drawables(im.level, im.root, d, n, ind, ptr)
+    view = np.eye(4, dtype=np.float32)
+    view[3, 2] = -50.0
+    f = 1.0 / np.tan(np.radians(30.0))
+    cv = lib.consumer_view(view.reshape(16), p11=f / (16 / 9), p22=f, p33=500.0 / (0.5 - 500.0),
+                           p43=0.5 * 500.0 / (0.5 - 500.0))
+    regions = [(dev.ptr, im.image.nbytes)]
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(warmup):
+        ctx.check_draws(ind, ptr, n, regions, cv, out)
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.check_draws(ind, ptr, n, regions, cv, out)
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / steps
+    got = ctx.download(out, lib.DRAW_CHECK_DTYPE, (n,))
+    g_ind = ctx.download(ind, np.uint32, (n, 4))
+    g_ptr = ctx.download(ptr, np.uint64, (n, 4))
+    k = 4096
+    ref = bind.check_draws([(im.image, im.base)], g_ind[:k], g_ptr[:k], cv, threads=bind.max_threads())
+    pulled = int(got["pulled"].astype(np.int64).sum())
+    return {"workload": f"{n} Tier A draws, {pulled} vertex pulls", "ms": ms,
+            "gpulls_per_s": pulled / (ms / 1e3) / 1e9, "draws_flagged": int((got["flags"] != 0).sum()),
+            "oracle_equal_first_4096": bool(np.array_equal(got[:k], ref))}
 
 
 def run_pack(ctx, im, steps: int, warmup: int, peak: float):

@@ -52,6 +52,33 @@ class Tuning(C.Structure):
                 ("reserved", u32)]
 
 
+class MemoryRegion(C.Structure):
+    _fields_ = [("base", u64), ("size", u64)]
+
+
+class ConsumerView(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("p11", C.c_float), ("p22", C.c_float), ("p33", C.c_float),
+                ("p43", C.c_float), ("p31", C.c_float), ("p32", C.c_float), ("p34", C.c_float),
+                ("p41", C.c_float), ("p42", C.c_float), ("p44", C.c_float), ("reserved", u32 * 2)]
+
+
+DRAW_CHECK_DTYPE = np.dtype([("checksum", np.uint64), ("pulled", np.uint32), ("flags", np.uint32)])
+DRAW_BAD_INDEX_READ, DRAW_BAD_VERTEX_READ, DRAW_BAD_MATRIX_LIST, DRAW_BAD_INSTANCE, DRAW_BAD_DRAWABLE_DATA = (
+    0x1, 0x2, 0x4, 0x8, 0x10)
+
+
+def consumer_view(view_matrix, p11, p22, p33, p43, p31=0.0, p32=0.0, p34=-1.0, p41=0.0, p42=0.0, p44=0.0):
+    """cadr_consumer_view from a column-major 4x4 view matrix (16 floats)
+    and the projection members of the consumer shader."""
+    v = ConsumerView()
+    m = np.ascontiguousarray(view_matrix, np.float32).reshape(16)
+    for k in range(16):
+        v.view[k] = float(m[k])
+    v.p11, v.p22, v.p33, v.p43 = p11, p22, p33, p43
+    v.p31, v.p32, v.p34, v.p41, v.p42, v.p44 = p31, p32, p34, p41, p42, p44
+    return v
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("max_inflight_batches", u32), ("max_batch_views", u32), ("window_ns", u64),
                 ("memory_budget_bytes", u64), ("reserve_bytes", u64)]
@@ -113,6 +140,7 @@ _SIGS = {
     "cadr_pack_repack": ([vp, vp], i32),
     "cadr_pack_patch": ([vp, vp, vp, u32, vp], i32),
     "cadr_pack_buffers": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(u32)], i32),
+    "cadr_check_draws": ([vp, vp, vp, u64, C.POINTER(MemoryRegion), u32, C.POINTER(ConsumerView), vp, vp], i32),
     "cadr_server_create": ([vp, C.POINTER(ServerConfig), C.POINTER(vp)], i32),
     "cadr_server_destroy": ([vp], i32),
     "cadr_server_submit": ([vp, vp, vp, u32, C.POINTER(u64)], i32),
@@ -298,6 +326,15 @@ class Context:
     def process_drawables(self, level: int, root: int, drawables, n: int, indirect, pointers, stream=None):
         check(self.lib.cadr_process_drawables(self.handle, level, root, _ptr(drawables), n,
                                               _ptr(indirect), _ptr(pointers), stream))
+
+    def check_draws(self, indirect, pointers, n: int, regions, view: "ConsumerView", out, stream=None):
+        """cadr_check_draws; regions: [(base, size)]; out: device buffer of
+        n DRAW_CHECK_DTYPE records."""
+        arr = (MemoryRegion * max(1, len(regions)))()
+        for k, (b, sz) in enumerate(regions):
+            arr[k].base, arr[k].size = b, sz
+        check(self.lib.cadr_check_draws(self.handle, _ptr(indirect), _ptr(pointers), n, arr, len(regions),
+                                        C.byref(view), _ptr(out), stream))
 
     def get_tuning(self) -> Tuning:
         t = Tuning()

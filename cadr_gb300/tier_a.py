@@ -12,7 +12,8 @@ everything the processDrawables pass dereferences:
     followed by the matrices (MatrixList.h:54-59).
 Vertex, index and drawable-data allocations are only resolved by the pass,
 never read, so their addresses point into a second region that the image
-does not hold.
+does not hold; with geometry_data=True the image holds them too (vertex
+positions, index buffers, MatrixList matrices), for the consumer check.
 
 Drawables are packed in the StateSet depth-first order of
 StateSet::recordToCommandBuffer (StateSet.cpp:198-262): a root StateSet with
@@ -55,7 +56,16 @@ class TierAImage:
     num_handles: int
 
 
-def _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles):
+# Consumer data per geometry (geometry_data=True): VERTICES positions of
+# 12 bytes and an index buffer of at most prims_per_geometry * 3000 indices.
+VERTICES = 1024
+
+
+def _geometry_bytes(prims_per_geometry):
+    return (VERTICES * 12 + prims_per_geometry * 3000 * 4 + 255) & ~255
+
+
+def _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles, geometry_data=False):
     """Handle count, table depth and region sizes of an image."""
     H = 3 * G + n + (n if with_drawable_data else 0) + extra_handles
     level = handle_level(H)
@@ -67,21 +77,28 @@ def _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, ext
     ml_stride = 64 + 64 * matrices_per_list
     ml_off = (tables_bytes + prims_bytes + 255) & ~255
     size = ml_off + n * ml_stride
+    if geometry_data:
+        size += G * _geometry_bytes(prims_per_geometry) + n * 64  # geometry, then drawable data
     return H, level, n_llt, n_rt, n_tables, tables_bytes, prims_bytes, ml_stride, ml_off, size
 
 
 def image_size(n: int, num_geometries: int | None = None, prims_per_geometry: int = 3,
-               with_drawable_data: bool = True, matrices_per_list: int = 1, extra_handles: int = 0) -> int:
+               with_drawable_data: bool = True, matrices_per_list: int = 1, extra_handles: int = 0,
+               geometry_data: bool = False) -> int:
     """Bytes of the image build() makes for the same arguments."""
     G = num_geometries or max(1, min(n, 4096))
-    return _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles)[-1]
+    return _layout(n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles, geometry_data)[-1]
 
 
 def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries: int | None = None,
           prims_per_geometry: int = 3, with_drawable_data: bool = True,
-          matrices_per_list: int = 1, extra_handles: int = 0) -> TierAImage:
+          matrices_per_list: int = 1, extra_handles: int = 0, geometry_data: bool = False) -> TierAImage:
     """Builds the image of n drawables.  base must be 256-byte aligned; it is
-    the device address the image will be uploaded to."""
+    the device address the image will be uploaded to.  With geometry_data
+    the vertex, index and drawable-data allocations lie inside the image:
+    per geometry VERTICES positions and an index buffer holding its
+    PrimitiveSets one after the other (PrimitiveSet.first counted within the
+    geometry), and the MatrixList matrices are filled."""
     assert base % 256 == 0
     G = num_geometries or max(1, min(n, 4096))
     idx = np.arange(max(n, 1), dtype=np.uint64)[:n]
@@ -94,7 +111,7 @@ def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries:
     h_ml = 1 + 3 * G + np.arange(n, dtype=np.uint64)
     h_dd = (1 + 3 * G + n + np.arange(n, dtype=np.uint64)) if with_drawable_data else np.zeros(n, np.uint64)
     H, level, n_llt, n_rt, n_tables, tables_bytes, prims_bytes, ml_stride, ml_off, size = _layout(
-        n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles)
+        n, G, prims_per_geometry, with_drawable_data, matrices_per_list, extra_handles, geometry_data)
     prims_off = tables_bytes
     img = np.zeros(size, np.uint8)
     tables = img[:tables_bytes].view(np.uint64).reshape(n_tables, TABLE)
@@ -102,12 +119,22 @@ def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries:
     # Addresses of every handle's target.
     addr = np.zeros(H + 1, np.uint64)
     far = np.uint64(base + ((size + (1 << 20)) & ~((1 << 20) - 1)))  # unbacked region
-    addr[h_vertex.astype(np.int64)] = far + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
-    addr[h_index.astype(np.int64)] = far + np.uint64(G << 16) + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
+    geo_off = ml_off + n * ml_stride
+    gb = _geometry_bytes(prims_per_geometry)
+    if geometry_data:
+        g_base = np.uint64(base + geo_off) + np.arange(G, dtype=np.uint64) * np.uint64(gb)
+        addr[h_vertex.astype(np.int64)] = g_base
+        addr[h_index.astype(np.int64)] = g_base + np.uint64(VERTICES * 12)
+    else:
+        addr[h_vertex.astype(np.int64)] = far + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
+        addr[h_index.astype(np.int64)] = far + np.uint64(G << 16) + np.arange(G, dtype=np.uint64) * np.uint64(1 << 16)
     addr[h_prims.astype(np.int64)] = np.uint64(base + prims_off) + np.arange(G, dtype=np.uint64) * np.uint64(prims_per_geometry * 8)
     addr[h_ml.astype(np.int64)] = np.uint64(base + ml_off) + idx * np.uint64(ml_stride)
     if with_drawable_data:
-        addr[h_dd.astype(np.int64)] = far + np.uint64(2 * G << 16) + idx * np.uint64(256)
+        if geometry_data:
+            addr[h_dd.astype(np.int64)] = np.uint64(base + geo_off + G * gb) + idx * np.uint64(64)
+        else:
+            addr[h_dd.astype(np.int64)] = far + np.uint64(2 * G << 16) + idx * np.uint64(256)
 
     # Last-level tables: llt k holds handles [k*2048, k*2048 + 2047].
     llt = tables[:n_llt].reshape(-1)
@@ -133,10 +160,31 @@ def build(n: int, seed: int, base: int, num_state_sets: int = 8, num_geometries:
     st = rng.Stream(seed, "tierA.prims")
     cnt = st.integers(np.arange(G * prims_per_geometry, dtype=np.uint64), 36, 3000).reshape(G, prims_per_geometry)
     ps[:, :, 0] = cnt
-    ps[:, :, 1] = np.cumsum(cnt.reshape(-1)).reshape(G, prims_per_geometry) - cnt
+    if geometry_data:
+        ps[:, :, 1] = np.cumsum(cnt, axis=1) - cnt
+    else:
+        ps[:, :, 1] = np.cumsum(cnt.reshape(-1)).reshape(G, prims_per_geometry) - cnt
     mlh = img[ml_off:ml_off + n * ml_stride].view(np.uint32).reshape(n, ml_stride // 4)
     mlh[:, 0] = matrices_per_list
     mlh[:, 1] = matrices_per_list
+    if geometry_data:
+        # Matrices: seeded affine transforms; positions in [-1, 1]^3;
+        # indices uniform over the geometry's vertices.
+        mats = img[ml_off:ml_off + n * ml_stride].view(np.float32).reshape(n, ml_stride // 4)[:, 16:]
+        m = rng.Stream(seed, "tierA.matrices").uniform_range(
+            np.arange(n * matrices_per_list * 16, dtype=np.uint64), -1.0, 1.0).astype(np.float32)
+        m = m.reshape(n * matrices_per_list, 4, 4)
+        m[:, 0:3, 3] = 0.0
+        m[:, 3, 3] = 1.0
+        m[:, 3, 0:3] *= 100.0
+        mats[...] = m.reshape(n, matrices_per_list * 16)
+        geo = img[geo_off:geo_off + G * gb].reshape(G, gb)
+        pos = rng.Stream(seed, "tierA.positions").uniform_range(
+            np.arange(G * VERTICES * 3, dtype=np.uint64), -1.0, 1.0).astype(np.float32)
+        geo[:, :VERTICES * 12] = pos.view(np.uint8).reshape(G, VERTICES * 12)
+        ni = prims_per_geometry * 3000
+        ind = rng.Stream(seed, "tierA.indices").integers(np.arange(G * ni, dtype=np.uint64), 0, VERTICES - 1)
+        geo[:, VERTICES * 12:VERTICES * 12 + ni * 4] = ind.astype(np.uint32).view(np.uint8).reshape(G, ni * 4)
 
     # Drawable records, grouped by StateSet (DFS order of the children).
     g_of = rng.Stream(seed, "tierA.geometry").integers(idx, 0, G - 1)

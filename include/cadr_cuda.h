@@ -258,6 +258,56 @@ CADR_API cadr_status cadr_pack_buffers(cadr_pack* pack, const cadr_drawable_gpu_
                                        const uint32_t** region_offsets, uint32_t* num_slots);
 
 /* ------------------------------------------------------------------------ */
+/* Vertex-pulling consumer check of the Tier A draws.  Replays, in CUDA, the
+ * reads of the vertex shader that consumes them
+ * (examples/RenderingPerformance/shader.vert:100-120): for draw i of
+ * cmdDrawIndirect, with dp = pointers[i] and cmd = indirect[i], for every
+ * instance m in [firstInstance, firstInstance + instanceCount) and vertex
+ * v = firstVertex + k, k < vertexCount:
+ *   index    = ((const uint32_t*)dp.index_data)[v]
+ *   position = ((const float[3]*)dp.vertex_data)[index]
+ *   eye      = (view * matrixList(dp.matrix_list).matrices[m]) * (position, 1)
+ *   gl_Position = (p11 ex + p31 ez + p41 ew, p22 ey + p32 ez + p42 ew,
+ *                  p33 ez + p43 ew, p34 ez + p44 ew),  eye3 = eye.xyz / eye.w
+ * (GLM operation order, every operation rounded once).  Every address is
+ * checked against `regions` (the device memory the draws may address) and
+ * against its alignment before it is read: a read that fails is skipped
+ * and flagged, so a bad draw buffer cannot fault the device.  Per draw:
+ * the (vertex, instance) pairs pulled, the flags, and the checksum: the sum
+ * modulo 2^64 over those pairs of
+ *   mix(X | Y << 32) ^ mix((Z | W << 32) ^ K) ^ mix((EX | EY << 32) ^ 2K)
+ *   ^ mix((EZ | index << 32) ^ 3K)
+ * with X..W the bits of gl_Position, EX..EZ those of eye3, K =
+ * 0x9E3779B97F4A7C15 and mix the SplitMix64 finaliser (order-independent,
+ * so any thread layout gives the same sum). */
+typedef struct cadr_memory_region {
+    uint64_t base;
+    uint64_t size;
+} cadr_memory_region;
+#define CADR_MAX_MEMORY_REGIONS 8u
+typedef struct cadr_consumer_view {
+    float view[16];                       /* SceneData.viewMatrix, column-major */
+    float p11, p22, p33, p43;             /* SceneData projection members */
+    float p31, p32, p34, p41, p42, p44;   /* specialization constants */
+    uint32_t reserved[2];
+} cadr_consumer_view;
+typedef struct cadr_draw_check {
+    uint64_t checksum;
+    uint32_t pulled;   /* (vertex, instance) pairs read and transformed */
+    uint32_t flags;    /* CADR_DRAW_* */
+} cadr_draw_check;
+#define CADR_DRAW_BAD_INDEX_READ 0x1u     /* an index read outside the regions or misaligned */
+#define CADR_DRAW_BAD_VERTEX_READ 0x2u    /* a position read outside the regions or misaligned */
+#define CADR_DRAW_BAD_MATRIX_LIST 0x4u    /* header or a matrix outside the regions, or not 64-byte aligned */
+#define CADR_DRAW_BAD_INSTANCE 0x8u       /* an instance index >= numMatrices */
+#define CADR_DRAW_BAD_DRAWABLE_DATA 0x10u /* non-null drawable data outside the regions or misaligned */
+CADR_API cadr_status cadr_check_draws(cadr_context* ctx, const cadr_draw_indirect_cmd* indirect,
+                                      const cadr_drawable_pointers* pointers, uint64_t num_draws,
+                                      const cadr_memory_region* regions, uint32_t num_regions,
+                                      const cadr_consumer_view* view, cadr_draw_check* out,
+                                      cadr_stream stream);
+
+/* ------------------------------------------------------------------------ */
 /* Tier B scenes. */
 CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc* desc,
                                        cadr_scene** out);

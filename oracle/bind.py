@@ -48,6 +48,8 @@ class OracleLib:
         L.oracle_max_threads.restype = i32
         L.oracle_pack_state_sets.argtypes = [u32, vp, u64, vp, vp, vp, vp, vp]
         L.oracle_pack_state_sets.restype = i32
+        L.oracle_check_draws.argtypes = [vp, u32, vp, vp, u64, vp, vp, i32]
+        L.oracle_check_draws.restype = i32
 
 
 def load() -> OracleLib:
@@ -172,6 +174,32 @@ def pack_state_sets(dfs_order, state_set_of_slot, list_index_of_slot, pool):
     if rc != 0:
         raise ValueError("oracle_pack_state_sets: the layout is not a set of lists")
     return packed, offsets
+
+
+class _Region(C.Structure):
+    _fields_ = [("bytes", C.c_void_p), ("base", C.c_uint64), ("size", C.c_uint64)]
+
+
+def check_draws(regions, indirect, pointers, view, threads: int = 0):
+    """The consumer check over host copies of device memory.  regions:
+    [(uint8 array, device base address)]; indirect uint32 [N,4]; pointers
+    uint64 [N,4]; view: a cadr_gb300.lib.ConsumerView.  Returns the
+    per-draw (checksum, pulled, flags) records."""
+    from cadr_gb300 import lib as cl
+    L = load().lib
+    arr = (_Region * max(1, len(regions)))()
+    keep = []
+    for k, (b, base) in enumerate(regions):
+        b = np.ascontiguousarray(b, np.uint8)
+        keep.append(b)
+        arr[k].bytes, arr[k].base, arr[k].size = b.ctypes.data, base, b.nbytes
+    ind = np.ascontiguousarray(indirect, np.uint32)
+    ptr = np.ascontiguousarray(pointers, np.uint64)
+    n = int(ind.shape[0])
+    out = np.zeros(n, cl.DRAW_CHECK_DTYPE)
+    L.oracle_check_draws(C.cast(arr, C.c_void_p), len(regions), _p(ind), _p(ptr), n, C.cast(C.pointer(view), C.c_void_p),
+                         _p(out), threads)
+    return out
 
 
 def valid_cmds(cmds: np.ndarray, counts: np.ndarray, offsets: np.ndarray) -> np.ndarray:

@@ -444,3 +444,137 @@ done:
     free(used);
     return rc;
 }
+
+/* ---- vertex-pulling consumer check (examples/RenderingPerformance/shader.vert:100-120) ---- */
+
+static int region_find(const oracle_region* r, uint32_t nr, uint64_t addr, uint64_t bytes, uint64_t align,
+                       const uint8_t** p)
+{
+    if (addr % align) return 0;
+    for (uint32_t k = 0; k < nr; k++) {
+        const uint64_t end = r[k].base + r[k].size;
+        if (addr >= r[k].base && addr <= end && bytes <= end - addr) {
+            *p = r[k].bytes + (addr - r[k].base);
+            return 1;
+        }
+    }
+    return 0;
+}
+
+static uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint32_t fbits32(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return u;
+}
+
+static uint64_t pair32(float lo, float hi) { return (uint64_t)fbits32(lo) | ((uint64_t)fbits32(hi) << 32); }
+
+/* r = ((a0*b.x + a1*b.y) + a2*b.z) + a3*b.w, one rounding per operation */
+static void col4(const float* a0, const float* a1, const float* a2, const float* a3, const float* b, float* r)
+{
+    for (int c = 0; c < 4; c++) {
+        volatile float t0 = a0[c] * b[0], t1 = a1[c] * b[1], t2 = a2[c] * b[2], t3 = a3[c] * b[3];
+        volatile float s0 = t0 + t1;
+        volatile float s1 = s0 + t2;
+        volatile float s2 = s1 + t3;
+        r[c] = s2;
+    }
+}
+
+static float mul(float a, float b)
+{
+    volatile float r = a * b;
+    return r;
+}
+static float add(float a, float b)
+{
+    volatile float r = a + b;
+    return r;
+}
+static float divf(float a, float b)
+{
+    volatile float r = a / b;
+    return r;
+}
+
+int oracle_check_draws(const oracle_region* regions, uint32_t nr, const cadr_draw_indirect_cmd* indirect,
+                       const cadr_drawable_pointers* pointers, uint64_t n, const cadr_consumer_view* v,
+                       cadr_draw_check* out, int threads)
+{
+    const uint64_t K = 0x9E3779B97F4A7C15ull;
+    const float* V = v->view;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (int64_t d = 0; d < (int64_t)n; d++) {
+        const cadr_draw_indirect_cmd cmd = indirect[d];
+        const cadr_drawable_pointers dp = pointers[d];
+        uint32_t flags = 0, pulled = 0;
+        uint64_t sum = 0;
+        const uint8_t* p;
+        if (dp.drawable_data_ptr && !region_find(regions, nr, dp.drawable_data_ptr, 64, 64, &p))
+            flags |= CADR_DRAW_BAD_DRAWABLE_DATA;
+        const uint8_t* mlp;
+        if (!region_find(regions, nr, dp.matrix_list_ptr, 64, 64, &mlp)) {
+            flags |= CADR_DRAW_BAD_MATRIX_LIST;
+        } else {
+            uint32_t num_matrices;
+            memcpy(&num_matrices, mlp, 4);
+            for (uint64_t m = cmd.first_instance; m < (uint64_t)cmd.first_instance + cmd.instance_count; m++) {
+                if (m >= num_matrices) {
+                    flags |= CADR_DRAW_BAD_INSTANCE;
+                    break;
+                }
+                const uint8_t* mp;
+                if (!region_find(regions, nr, dp.matrix_list_ptr + 64 + 64 * m, 64, 16, &mp)) {
+                    flags |= CADR_DRAW_BAD_MATRIX_LIST;
+                    continue;
+                }
+                float M[16], W[16];
+                memcpy(M, mp, 64);
+                for (int c = 0; c < 4; c++) col4(V, V + 4, V + 8, V + 12, M + 4 * c, W + 4 * c);
+                /* the GPU's lanes stop at their first bad index read; lane l
+                 * reads k = l, l + 32, ... */
+                for (uint32_t lane = 0; lane < 32; lane++) {
+                    for (uint64_t k = lane; k < cmd.vertex_count; k += 32) {
+                        const uint8_t* ip;
+                        if (!region_find(regions, nr, dp.index_data_ptr + 4ull * ((uint64_t)cmd.first_vertex + k), 4, 4, &ip)) {
+                            flags |= CADR_DRAW_BAD_INDEX_READ;
+                            break;
+                        }
+                        uint32_t index;
+                        memcpy(&index, ip, 4);
+                        const uint8_t* vp;
+                        if (!region_find(regions, nr, dp.vertex_data_ptr + 12ull * index, 12, 4, &vp)) {
+                            flags |= CADR_DRAW_BAD_VERTEX_READ;
+                            continue;
+                        }
+                        float pos[4];
+                        memcpy(pos, vp, 12);
+                        pos[3] = 1.0f;
+                        float e[4];
+                        col4(W, W + 4, W + 8, W + 12, pos, e);
+                        const float gx = add(add(mul(v->p11, e[0]), mul(v->p31, e[2])), mul(v->p41, e[3]));
+                        const float gy = add(add(mul(v->p22, e[1]), mul(v->p32, e[2])), mul(v->p42, e[3]));
+                        const float gz = add(mul(v->p33, e[2]), mul(v->p43, e[3]));
+                        const float gw = add(mul(v->p34, e[2]), mul(v->p44, e[3]));
+                        const float ex = divf(e[0], e[3]), ey = divf(e[1], e[3]), ez = divf(e[2], e[3]);
+                        sum += mix64(pair32(gx, gy)) ^ mix64(pair32(gz, gw) ^ K) ^ mix64(pair32(ex, ey) ^ (2 * K)) ^
+                               mix64(((uint64_t)fbits32(ez) | ((uint64_t)index << 32)) ^ (3 * K));
+                        pulled++;
+                    }
+                }
+            }
+        }
+        out[d].checksum = sum;
+        out[d].pulled = pulled;
+        out[d].flags = flags;
+    }
+    return 0;
+}

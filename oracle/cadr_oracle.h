@@ -62,6 +62,13 @@ int oracle_pack_state_sets(uint32_t S, const uint32_t* dfs_order, uint64_t n, co
                            const uint32_t* list_index_of_slot, const cadr_drawable_gpu_data* pool,
                            cadr_drawable_gpu_data* packed, uint32_t* offsets);
 
+/* The vertex-pulling consumer check of cadr_check_draws, over host copies
+ * of the device memory regions: same reads, same arithmetic, same flags
+ * and checksums (see include/cadr_cuda.h). */
+int oracle_check_draws(const oracle_region* regions, uint32_t num_regions, const cadr_draw_indirect_cmd* indirect,
+                       const cadr_drawable_pointers* pointers, uint64_t n, const cadr_consumer_view* view,
+                       cadr_draw_check* out, int threads);
+
 /* GLM-order 4x4 product out = a * b (column-major float[16]). */
 void oracle_mat4_mul(const float* a, const float* b, float* out);
 /* BoundingSphere operator*: out = m * (cx, cy, cz, r). */

@@ -349,3 +349,85 @@ def test_pack_state_sets_rejects_bad_layouts():
         bind.pack_state_sets([0, 0], [0, 0, 1], [0, 1, 0], pool)   # not a permutation
     with pytest.raises(ValueError):
         bind.pack_state_sets([0, 1], [0, 0, 1], [0, 2, 0], pool)   # index past the list
+
+
+def _mix64(z):
+    M = (1 << 64) - 1
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return z ^ (z >> 31)
+
+
+def _consumer_image():
+    """One MatrixList (header + 1 matrix), an index buffer and 3 vertices
+    at device address B."""
+    B = 1 << 32
+    img = np.zeros(1024, np.uint8)
+    img[0:4] = np.array([1], np.uint32).view(np.uint8)             # numMatrices
+    M = np.eye(4, dtype=np.float32)
+    M[3, 0:3] = [1.0, 2.0, 3.0]                                    # column 3: translation
+    M[0, 0] = 2.0
+    img[64:128] = M.reshape(16).view(np.uint8)
+    img[256:268] = np.array([2, 0, 1], np.uint32).view(np.uint8)
+    pos = np.array([[0.5, -1.0, 0.25], [1.5, 0.75, -2.0], [-0.125, 3.0, 1.0]], np.float32)
+    img[512:548] = pos.reshape(9).view(np.uint8)
+    ind = np.array([[3, 1, 0, 0]], np.uint32)
+    ptr = np.array([[B + 512, B + 256, B, 0]], np.uint64)
+    return B, img, ind, ptr, M, pos
+
+
+def test_consumer_check_known_answer():
+    """The oracle's consumer check on a hand-built draw equals the shader
+    arithmetic (shader.vert:100-120) done here step by step in float32."""
+    from cadr_gb300 import lib
+    from oracle import bind
+    B, img, ind, ptr, M, pos = _consumer_image()
+    view = np.eye(4, dtype=np.float32)
+    view[3, 2] = -10.0
+    p = dict(p11=1.5, p22=2.0, p33=-1.0, p43=-0.2, p31=0.0, p32=0.0, p34=-1.0, p41=0.0, p42=0.0, p44=0.0)
+    v = lib.consumer_view(view.reshape(16), **p)
+    out = bind.check_draws([(img, B)], ind, ptr, v)
+    f = np.float32
+
+    def col(a, b):  # ((a0 b.x + a1 b.y) + a2 b.z) + a3 b.w, rounded each step
+        return np.array([f(f(f(f(a[0][c] * b[0]) + f(a[1][c] * b[1])) + f(a[2][c] * b[2])) + f(a[3][c] * b[3]))
+                         for c in range(4)], np.float32)
+    W = [col(view, M[c]) for c in range(4)]
+    K = 0x9E3779B97F4A7C15
+    bits = lambda x: int(np.float32(x).view(np.uint32))
+    total = 0
+    for k in range(3):
+        index = int(np.frombuffer(img[256:268].tobytes(), np.uint32)[k])
+        e = col(W, np.array([*pos[index], 1.0], np.float32))
+        gx = f(f(f(p["p11"]) * e[0]) + f(f(p["p31"]) * e[2])) + f(f(p["p41"]) * e[3])
+        gy = f(f(f(p["p22"]) * e[1]) + f(f(p["p32"]) * e[2])) + f(f(p["p42"]) * e[3])
+        gz = f(f(p["p33"]) * e[2]) + f(f(p["p43"]) * e[3])
+        gw = f(f(p["p34"]) * e[2]) + f(f(p["p44"]) * e[3])
+        ex, ey, ez = f(e[0] / e[3]), f(e[1] / e[3]), f(e[2] / e[3])
+        h = (_mix64(bits(gx) | bits(gy) << 32) ^ _mix64((bits(gz) | bits(gw) << 32) ^ K)
+             ^ _mix64((bits(ex) | bits(ey) << 32) ^ (2 * K % (1 << 64)))
+             ^ _mix64((bits(ez) | index << 32) ^ (3 * K % (1 << 64))))
+        total = (total + h) % (1 << 64)
+    assert int(out["checksum"][0]) == total and out["pulled"][0] == 3 and out["flags"][0] == 0
+
+
+@pytest.mark.parametrize("case,flag", [("index outside", 0x1), ("vertex misaligned", 0x2), ("list outside", 0x4),
+                                       ("instance past list", 0x8), ("drawable data misaligned", 0x10)])
+def test_consumer_check_flags(case, flag):
+    from cadr_gb300 import lib
+    from oracle import bind
+    B, img, ind, ptr, _, _ = _consumer_image()
+    ind, ptr = ind.copy(), ptr.copy()
+    if case == "index outside":
+        ptr[0, 1] = B + 4096
+    elif case == "vertex misaligned":
+        ptr[0, 0] = B + 514
+    elif case == "list outside":
+        ptr[0, 2] = B + 8192
+    elif case == "instance past list":
+        ind[0, 1] = 2
+    else:
+        ptr[0, 3] = B + 8
+    v = lib.consumer_view(np.eye(4, dtype=np.float32).reshape(16), 1.0, 1.0, -1.0, -0.2)
+    out = bind.check_draws([(img, B)], ind, ptr, v)
+    assert out["flags"][0] == flag
