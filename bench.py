@@ -628,7 +628,16 @@ def main():
     prop_ms = float(np.mean([f[0] for f in frames])) if frames else None
     stream_ms = float(np.mean([f[3] for f in frames])) if frames else None
 
+    out_ref = out.fetch()  # the device-resident pass's result, to check the e2e read-back against
+
     # ---- end to end through the C ABI with host buffers -------------------
+    # Every step uploads all per-drawable and level inputs from pinned host
+    # memory, culls, and reads back the counts and the valid command prefix
+    # of every StateSet.  Two device scenes alternate, so that a step's
+    # uploads (upload stream) overlap the previous step's pass and read-back
+    # (compute stream); the scenes' own ordering events keep every upload
+    # behind the pass that reads the scene before it, with no host sync.
+    import torch
     e2e_steps = args.e2e_steps or min(args.steps, 50)
     pin = {}
     for name, a in [("local", sc.local), ("parent", sc.parent), ("sphere", sc.sphere), ("geometry", sc.geometry)]:
@@ -644,39 +653,67 @@ def main():
             bp = lib.PinnedBuffer(par.nbytes)
             bp.view(par.dtype, par.shape)[...] = par
         lvl_pin.append((bl, bp, loc.shape[0]))
-    h_counts = lib.PinnedBuffer(sc.num_state_sets * 4)
-    h_cmds = lib.PinnedBuffer(sc.n * 20)
+    pair = [ds, lib.DeviceScene(ctx, sc)]
+    outs = [out, lib.CullOutputs(ctx, sc.n, sc.num_state_sets)]
+    h_counts = [lib.PinnedBuffer(sc.num_state_sets * 4) for _ in range(2)]
+    h_cmds = [lib.PinnedBuffer(sc.n * 20) for _ in range(2)]
+    counts_ready = [torch.cuda.Event() for _ in range(2)]
+    cstream = torch.cuda.ExternalStream(ctx.stream)
     offs = sc.state_set_offsets.astype(np.int64)
     h2d = sum(b.nbytes for b in pin.values()) + sum(bl.nbytes + (bp.nbytes if bp else 0) for bl, bp, _ in lvl_pin)
 
-    def e2e_step():
+    def e2e_upload(k):
+        d = pair[k % 2]
         for l, (bl, bp, n_l) in enumerate(lvl_pin):
-            lib.check(L.cadr_scene_upload_level(ds.handle, l, bl.ptr, bp.ptr if bp else None, 0, n_l))
-        lib.check(L.cadr_scene_upload_drawables(ds.handle, pin["local"].ptr, pin["parent"].ptr,
+            lib.check(L.cadr_scene_upload_level(d.handle, l, bl.ptr, bp.ptr if bp else None, 0, n_l))
+        lib.check(L.cadr_scene_upload_drawables(d.handle, pin["local"].ptr, pin["parent"].ptr,
                                                 pin["sphere"].ptr, pin["geometry"].ptr, 0, sc.n))
-        ds.cull(view, out)
-        lib.check(L.cadr_download(ctx.handle, h_counts.ptr, out.counts.ptr, sc.num_state_sets * 4, None))
-        lib.check(L.cadr_stream_synchronize(ctx.stream))
-        cnt = h_counts.view(np.uint32, (sc.num_state_sets,))
+
+    def e2e_cull(k):
+        j = k % 2
+        pair[j].cull(view, outs[j])
+        lib.check(L.cadr_download(ctx.handle, h_counts[j].ptr, outs[j].counts.ptr, sc.num_state_sets * 4, None))
+        counts_ready[j].record(cstream)
+
+    def e2e_readback(k):
+        j = k % 2
+        counts_ready[j].synchronize()
+        cnt = h_counts[j].view(np.uint32, (sc.num_state_sets,))
         d2h = sc.num_state_sets * 4
         for s in range(sc.num_state_sets):
             c = int(cnt[s])
             if c:
-                lib.check(L.cadr_download(ctx.handle, h_cmds.ptr + int(offs[s]) * 20,
-                                          out.cmds.ptr + int(offs[s]) * 20, c * 20, None))
+                lib.check(L.cadr_download(ctx.handle, h_cmds[j].ptr + int(offs[s]) * 20,
+                                          outs[j].cmds.ptr + int(offs[s]) * 20, c * 20, None))
                 d2h += c * 20
+        return d2h
+
+    def e2e_run(steps):
+        d2h = 0
+        e2e_upload(0)
+        for k in range(steps):
+            e2e_cull(k)
+            if k + 1 < steps:
+                e2e_upload(k + 1)
+            d2h += e2e_readback(k)
         lib.check(L.cadr_stream_synchronize(ctx.stream))
         return d2h
 
-    for _ in range(2):
-        e2e_step()
+    e2e_run(3)
     barrier()
     t1 = time.perf_counter()
-    d2h_total = 0
-    for _ in range(e2e_steps):
-        d2h_total += e2e_step()
+    d2h_total = e2e_run(e2e_steps)
     e2e_s = (time.perf_counter() - t1) / e2e_steps
     barrier()
+    # The last step's read-back equals the device-resident pass's result.
+    j = (e2e_steps - 1) % 2
+    got_counts = h_counts[j].view(np.uint32, (sc.num_state_sets,)).copy()
+    got_cmds = h_cmds[j].view(np.uint32, (sc.n, 5))
+    ref_cmds = np.ascontiguousarray(out_ref["cmds"]).view(np.uint32).reshape(sc.n, 5)
+    e2e_same = bool(np.array_equal(got_counts, out_ref["counts"]) and all(
+        np.array_equal(got_cmds[int(offs[s]):int(offs[s]) + int(got_counts[s])],
+                       ref_cmds[int(offs[s]):int(offs[s]) + int(got_counts[s])])
+        for s in range(sc.num_state_sets)))
     clk = clocks.stop()
     e2e_value = world * sc.n / e2e_s / 1e9
 
@@ -709,7 +746,9 @@ def main():
                  "step_algorithmic_bytes": step_algorithmic_bytes(sc, visible),
                  "step_gbs": step_algorithmic_bytes(sc, visible) / (ms / 1e3) / 1e9},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h_total // max(1, e2e_steps), "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": d2h_total // max(1, e2e_steps), "ms_per_step": e2e_s * 1e3,
+                "pipelining": "two device scenes alternate; a step's uploads overlap the previous step's pass and read-back",
+                "readback_equals_device_pass": e2e_same},
         "gpu_launches": launches,
         "clocks": clk,
         "scene_generation_s": gen_s,

@@ -330,6 +330,10 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
     }
     ctx->launches++;
     B.scratch.launches++;
+    for (uint32_t v = 0; v < num_views; v++) {
+        cadr_status st = scene_mark_read(views[v].scene, s);
+        if (st != CADR_OK) return st;
+    }
     e = cudaEventRecord(B.jobs_free, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull_batched: record");
     B.jobs_pending = true;

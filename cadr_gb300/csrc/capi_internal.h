@@ -53,6 +53,8 @@ struct cadr_scene {
     bool committed = false;
     bool upload_pending = false;
     cudaEvent_t uploaded = nullptr;
+    bool read_pending = false;
+    cudaEvent_t read_done = nullptr;       // recorded after the last pass that reads the scene
 };
 
 namespace cadr {
@@ -67,6 +69,9 @@ cadr_status upload_bytes(cadr_context* ctx, void* dst, const void* src, size_t b
 cudaStream_t pick_stream(cadr_context* ctx, cadr_stream s);
 void destroy_batched_state(cadr_context* ctx);
 cadr_status scene_prepare(cadr_scene* sc, cudaStream_t stream);
+// After a pass on `stream` that reads the scene: later uploads into the
+// scene wait for it.
+cadr_status scene_mark_read(cadr_scene* sc, cudaStream_t stream);
 ViewConst to_view_const(const cadr_view& v);
 cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, ViewJob* jobs, uint64_t* total);
 cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream);

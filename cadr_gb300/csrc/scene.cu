@@ -51,6 +51,24 @@ cadr_status scene_prepare(cadr_scene* sc, cudaStream_t stream)
     return CADR_OK;
 }
 
+cadr_status scene_mark_read(cadr_scene* sc, cudaStream_t stream)
+{
+    cudaError_t e = cudaEventRecord(sc->read_done, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "scene: record read");
+    sc->read_pending = true;
+    return CADR_OK;
+}
+
+// Uploads go to the context's upload stream; an upload into a scene waits
+// there for the passes issued before it that read the scene.
+static cadr_status before_upload(cadr_scene* sc)
+{
+    if (!sc->read_pending) return CADR_OK;
+    cudaError_t e = cudaStreamWaitEvent(sc->ctx->upload_stream, sc->read_done, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "scene upload: wait for readers");
+    return CADR_OK;
+}
+
 static cadr_status after_upload(cadr_scene* sc)
 {
     cudaError_t e = cudaEventRecord(sc->uploaded, sc->ctx->upload_stream);
@@ -138,6 +156,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     cudaSetDevice(ctx->device);
     cudaError_t e = cudaMalloc(&sc->arena, off ? off : 256);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sc->uploaded, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sc->read_done, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cadr_scene_destroy(sc);
         return cuda_fail(e, "scene_create: device memory");
@@ -176,6 +195,7 @@ CADR_API cadr_status cadr_scene_destroy(cadr_scene* sc)
     cudaDeviceSynchronize();
     if (sc->arena) cudaFree(sc->arena);
     if (sc->uploaded) cudaEventDestroy(sc->uploaded);
+    if (sc->read_done) cudaEventDestroy(sc->read_done);
     delete sc;
     return CADR_OK;
 }
@@ -196,7 +216,8 @@ CADR_API cadr_status cadr_scene_upload_level(cadr_scene* sc, uint32_t level, con
     if (first > n || count > n - first) return fail(CADR_ERR_INVALID_ARG, "scene_upload_level: rows out of range");
     if (level == 0 && parent) return fail(CADR_ERR_INVALID_ARG, "scene_upload_level: level 0 has no parents");
     cadr_context* ctx = sc->ctx;
-    cadr_status st = CADR_OK;
+    cadr_status st = before_upload(sc);
+    if (st != CADR_OK) return st;
     if (local) st = upload_bytes(ctx, sc->buf.level_local[level] + first * 16, local, count * 64, ctx->upload_stream);
     if (st == CADR_OK && parent)
         st = upload_bytes(ctx, sc->buf.level_parent[level] + first, parent, count * 4, ctx->upload_stream);
@@ -213,7 +234,8 @@ CADR_API cadr_status cadr_scene_upload_drawables(cadr_scene* sc, const float* lo
     if (first > n || count > n - first) return fail(CADR_ERR_INVALID_ARG, "scene_upload_drawables: rows out of range");
     if (parent && !sc->desc.num_levels) return fail(CADR_ERR_INVALID_ARG, "scene_upload_drawables: scene has no hierarchy");
     cadr_context* ctx = sc->ctx;
-    cadr_status st = CADR_OK;
+    cadr_status st = before_upload(sc);
+    if (st != CADR_OK) return st;
     if (local) st = upload_bytes(ctx, sc->buf.local + first * 16, local, count * 64, ctx->upload_stream);
     if (st == CADR_OK && parent) st = upload_bytes(ctx, sc->buf.parent + first, parent, count * 4, ctx->upload_stream);
     if (st == CADR_OK && sphere) st = upload_bytes(ctx, sc->buf.sphere + first * 4, sphere, count * 16, ctx->upload_stream);
@@ -231,7 +253,8 @@ CADR_API cadr_status cadr_scene_upload_state_sets(cadr_scene* sc, const uint32_t
         return fail(CADR_ERR_INVALID_ARG, "scene_upload_state_sets: offsets must start at 0 and end at N");
     for (uint32_t s = 0; s < S; s++)
         if (offsets[s + 1] < offsets[s]) return fail(CADR_ERR_INVALID_ARG, "scene_upload_state_sets: offsets not sorted");
-    cadr_status st = upload_bytes(sc->ctx, sc->buf.state_set_offsets, offsets, (size_t)(S + 1) * 4, sc->ctx->upload_stream);
+    cadr_status st = before_upload(sc);
+    if (st == CADR_OK) st = upload_bytes(sc->ctx, sc->buf.state_set_offsets, offsets, (size_t)(S + 1) * 4, sc->ctx->upload_stream);
     if (st != CADR_OK) return st;
     sc->committed = false;
     return after_upload(sc);
@@ -240,7 +263,9 @@ CADR_API cadr_status cadr_scene_upload_state_sets(cadr_scene* sc, const uint32_t
 CADR_API cadr_status cadr_scene_upload_lods(cadr_scene* sc, const cadr_lod* lods)
 {
     if (!sc || !lods) return fail(CADR_ERR_INVALID_ARG, "scene_upload_lods: null argument");
-    cadr_status st = upload_bytes(sc->ctx, sc->buf.lods, lods,
+    cadr_status st = before_upload(sc);
+    if (st != CADR_OK) return st;
+    st = upload_bytes(sc->ctx, sc->buf.lods, lods,
                                   (size_t)sc->desc.num_geometries * sc->desc.num_lods * 16, sc->ctx->upload_stream);
     if (st != CADR_OK) return st;
     return after_upload(sc);
@@ -265,7 +290,7 @@ CADR_API cadr_status cadr_scene_propagate(cadr_scene* sc, int write_world_sphere
     cudaError_t e = launch_leaf_propagate(a, s);
     if (e != cudaSuccess) return cuda_fail(e, "scene_propagate: launch");
     if (a.n) sc->ctx->launches++;
-    return CADR_OK;
+    return scene_mark_read(sc, s);
 }
 
 CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_indexed_cmd* cmds, uint32_t* counts,
@@ -316,7 +341,7 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     e = cudaEventRecord(ctx->pass_done, s);
     if (e != cudaSuccess) return cuda_fail(e, "cull: record");
     ctx->pass_recorded = true;
-    return CADR_OK;
+    return scene_mark_read(sc, s);
 }
 
 }  // extern "C"

@@ -102,7 +102,7 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
     e = launch_leaf_cull(a, scratch, s, nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: launch");
     ctx->launches += kLeafCullLaunches;
-    return CADR_OK;
+    return scene_mark_read(sc, s);
 }
 
 }  // extern "C"

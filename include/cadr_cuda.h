@@ -314,7 +314,14 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
 CADR_API cadr_status cadr_scene_destroy(cadr_scene* scene);
 CADR_API cadr_status cadr_scene_get_buffers(cadr_scene* scene, cadr_scene_buffers* out);
 /* Host uploads of scene inputs (rows [first, first+count) of one array).
- * `parent` may be NULL to leave the parent array untouched. */
+ * `parent` may be NULL to leave the parent array untouched.  Uploads run
+ * on the context's upload stream in call order.  An upload waits there for
+ * the passes issued before it that read the scene (cadr_cull,
+ * cadr_cull_static_scratch, cadr_scene_propagate, cadr_cull_batched), and
+ * the passes issued after it wait for the upload, so a frame loop may
+ * upload the next frame's inputs without synchronising.  Scenes served by a
+ * cadr_server are read on the server's own streams: drain the server
+ * before uploading into them. */
 CADR_API cadr_status cadr_scene_upload_level(cadr_scene* scene, uint32_t level,
                                              const float* local, const uint32_t* parent,
                                              uint64_t first, uint64_t count);

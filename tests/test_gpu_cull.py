@@ -115,6 +115,51 @@ def test_tile_scan_spans_chunks(ctx):
     assert_same(res, ref, sc.state_set_offsets)
 
 
+def test_upload_after_cull_is_ordered(ctx):
+    """A frame loop without synchronisation: cull, upload the next frame's
+    inputs into the same scene from pinned memory, cull again.  The first
+    pass must see the old inputs and the second the new ones: the upload
+    waits for the first pass, the second pass for the upload."""
+    import dataclasses
+    a = scenes.config2(n=1 << 22, seed=1)
+    b = scenes.config2(n=1 << 22, seed=2)
+    # The second frame: b's per-drawable and level inputs over a's
+    # StateSets and LOD table (the uploads below leave those).
+    ab = dataclasses.replace(a, level_local=b.level_local, level_parent=b.level_parent, local=b.local,
+                             parent=b.parent, sphere=b.sphere, geometry=b.geometry)
+    view = a.views[0]
+    ref1, ref2 = bind.cull(a, view), bind.cull(ab, view)
+    pin = {}
+    for name in ("local", "parent", "sphere", "geometry"):
+        arr = getattr(b, name)
+        pb = lib.PinnedBuffer(arr.nbytes)
+        pb.view(arr.dtype, arr.shape)[...] = arr
+        pin[name] = pb
+    lv = []
+    for loc, par in zip(b.level_local, b.level_parent):
+        pl = lib.PinnedBuffer(loc.nbytes)
+        pl.view(loc.dtype, loc.shape)[...] = loc
+        pp = None
+        if par is not None:
+            pp = lib.PinnedBuffer(par.nbytes)
+            pp.view(par.dtype, par.shape)[...] = par
+        lv.append((pl, pp, loc.shape[0]))
+    ds = lib.DeviceScene(ctx, a)
+    ctx.sync()
+    out1 = lib.CullOutputs(ctx, a.n, a.num_state_sets)
+    out2 = lib.CullOutputs(ctx, a.n, a.num_state_sets)
+    L = ctx.lib
+    ds.cull(view, out1)
+    for l, (pl, pp, n_l) in enumerate(lv):
+        lib.check(L.cadr_scene_upload_level(ds.handle, l, pl.ptr, pp.ptr if pp else None, 0, n_l))
+    lib.check(L.cadr_scene_upload_drawables(ds.handle, pin["local"].ptr, pin["parent"].ptr, pin["sphere"].ptr,
+                                            pin["geometry"].ptr, 0, a.n))
+    ds.cull(view, out2)
+    ctx.sync()
+    assert_same(out1.fetch(), ref1, a.state_set_offsets)
+    assert_same(out2.fetch(), ref2, a.state_set_offsets)
+
+
 def test_staged_upload_path_equals_pinned(ctx):
     """Host inputs from pageable memory go through the pinned ring on the
     side stream; from pinned memory they are copied directly: same result."""
