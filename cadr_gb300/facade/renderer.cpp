@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <unordered_set>
 
 namespace CadR {
 
@@ -61,6 +62,7 @@ void Drawable::destroy() noexcept
 StateSet::~StateSet()
 {
     for (Drawable* d : _drawables) d->_index = ~0u;
+    for (uint32_t s : _slots) _renderer->freeSlot(s);
 }
 
 void StateSet::removeChild(StateSet& child)
@@ -75,6 +77,7 @@ void StateSet::append(Drawable& d, const DrawableGpuData& g)
     d._index = uint32_t(_records.size());
     _records.push_back(g);
     _drawables.push_back(&d);
+    _slots.push_back(_renderer->allocSlot(this, g));
 }
 
 // O(1) removal: the last record takes the removed one's place.
@@ -82,14 +85,17 @@ void StateSet::remove(Drawable& d) noexcept
 {
     const uint32_t i = d._index;
     const size_t last = _records.size() - 1;
+    _renderer->freeSlot(_slots[i]);
     if (i != last) {
         _records[i] = _records[last];
         Drawable* moved = _drawables[last];
         _drawables[i] = moved;
         moved->_index = i;
+        _slots[i] = _slots[last];
     }
     _records.pop_back();
     _drawables.pop_back();
+    _slots.pop_back();
     d._index = ~0u;
 }
 
@@ -119,6 +125,19 @@ void StateSet::recordToCommandBuffer(std::vector<DrawCall>& out, size_t& counter
     for (StateSet* c : childList) c->recordToCommandBuffer(out, counter);
 }
 
+void StateSet::recordDrawCalls(std::vector<DrawCall>& out, size_t& counter) const
+{
+    if (_skipRecording) return;
+    const size_t n = _records.size();
+    if (n > 0) {
+        out.push_back(DrawCall{this, counter, uint32_t(n),
+                               _renderer->drawablePointersBufferAddress() + counter * Renderer::drawablePointersRecordSize,
+                               counter * sizeof(cadr_draw_indirect_cmd)});
+        counter += n;
+    }
+    for (const StateSet* c : childList) c->recordDrawCalls(out, counter);
+}
+
 // ---------------------------------------------------------------------------
 // Renderer.
 
@@ -138,6 +157,7 @@ Renderer::Renderer(MemoryBackend& backend) : _backend(&backend)
 Renderer::~Renderer()
 {
     if (_ownContext) cadr_context_synchronize(_ownContext);
+    if (_pack) cadr_pack_destroy(_pack);
     if (_drawables) _backend->freeBlock(_drawables);
     if (_indirect) _backend->freeBlock(_indirect);
     if (_pointers) _backend->freeBlock(_pointers);
@@ -210,6 +230,136 @@ void Renderer::processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr
     recordSceneRendering(root, out);
     executeCopyOperations();
     recordDrawableProcessing(n, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident records.
+
+uint32_t Renderer::allocSlot(StateSet* owner, const DrawableGpuData& g)
+{
+    uint32_t s;
+    if (!_freeSlots.empty()) {
+        s = _freeSlots.back();
+        _freeSlots.pop_back();
+        _slotOwner[s] = owner;
+    } else {
+        s = uint32_t(_slotOwner.size());
+        _slotOwner.push_back(owner);
+    }
+    _newSlots.push_back(s);
+    _newRecords.push_back(g);
+    _layoutDirty = true;
+    return s;
+}
+
+void Renderer::freeSlot(uint32_t s) noexcept
+{
+    _slotOwner[s] = nullptr;
+    _freeSlots.push_back(s);
+    _layoutDirty = true;
+}
+
+// A larger pack: every live record is queued again (from the StateSets'
+// host lists, which stay authoritative).
+void Renderer::growPack(uint32_t slots)
+{
+    cadr_context* ctx = _backend->context();
+    const uint32_t cap = std::max<uint32_t>(1024u, uint32_t(slots + slots / 2));
+    cadr_pack* p = nullptr;
+    check(cadr_pack_create(ctx, cap, &p), "Renderer: pack");
+    if (_pack) {
+        cadr_context_synchronize(ctx);
+        cadr_pack_destroy(_pack);
+    }
+    _pack = p;
+    _packCapacity = cap;
+    _newSlots.clear();
+    _newRecords.clear();
+    std::vector<bool> seen(_slotOwner.size(), false);
+    for (uint32_t s = 0; s < _slotOwner.size(); s++) {
+        StateSet* ss = _slotOwner[s];
+        if (!ss || seen[s]) continue;
+        for (size_t li = 0; li < ss->_slots.size(); li++) {
+            seen[ss->_slots[li]] = true;
+            _newSlots.push_back(ss->_slots[li]);
+            _newRecords.push_back(ss->_records[li]);
+        }
+    }
+    _layoutDirty = true;
+}
+
+void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream)
+{
+    cadr_context* ctx = _backend->context();
+    if (!ctx) throw LogicError("Renderer::processDrawablesResident(): this renderer has no CUDA context");
+    // A StateSet reached twice (a child of two parents) is recorded twice,
+    // which one slot per record cannot express: such a frame takes the
+    // copying path.
+    {
+        std::unordered_set<const StateSet*> seen;
+        std::vector<const StateSet*> stack{&root};
+        while (!stack.empty()) {
+            const StateSet* ss = stack.back();
+            stack.pop_back();
+            if (!seen.insert(ss).second) {
+                processDrawables(root, out, stream);
+                return;
+            }
+            for (const StateSet* c : ss->childList) stack.push_back(c);
+        }
+    }
+    const size_t n = prepareSceneRendering(root);
+    size_t counter = 0;
+    root.recordDrawCalls(out, counter);
+    executeCopyOperations();
+    const uint32_t slots = uint32_t(_slotOwner.size());
+    if (slots > _packCapacity) growPack(slots);
+    if (_layoutDirty) {
+        // StateSets in recording order, depth-first from the root; every slot
+        // not reached from it (free, or in a StateSet outside the tree) goes
+        // to one trailing set that is never drawn.
+        std::vector<uint32_t> setOf(slots, ~0u), indexOf(slots, 0);
+        uint32_t id = 0;
+        std::vector<const StateSet*> stack{&root};
+        while (!stack.empty()) {
+            const StateSet* ss = stack.back();
+            stack.pop_back();
+            for (size_t li = 0; li < ss->_slots.size(); li++) {
+                setOf[ss->_slots[li]] = id;
+                indexOf[ss->_slots[li]] = uint32_t(li);
+            }
+            id++;
+            for (auto it = ss->childList.rbegin(); it != ss->childList.rend(); ++it) stack.push_back(*it);
+        }
+        uint32_t rest = 0;
+        for (uint32_t s = 0; s < slots; s++)
+            if (setOf[s] == ~0u) {
+                setOf[s] = id;
+                indexOf[s] = rest++;
+            }
+        std::vector<uint32_t> dfs(id + 1);
+        for (uint32_t k = 0; k <= id; k++) dfs[k] = k;
+        check(cadr_pack_set_layout(_pack, slots, id + 1, dfs.data(), setOf.data(), indexOf.data(), stream),
+              "Renderer: pack layout");
+    }
+    if (!_newSlots.empty()) {
+        check(cadr_pack_patch(_pack, _newSlots.data(), reinterpret_cast<const cadr_drawable_gpu_data*>(_newRecords.data()),
+                              uint32_t(_newSlots.size()), stream),
+              "Renderer: new records");
+        _newSlots.clear();
+        _newRecords.clear();
+    }
+    if (_layoutDirty) {
+        check(cadr_pack_repack(_pack, stream), "Renderer: repack");
+        _layoutDirty = false;
+    }
+    if (n == 0) return;
+    const cadr_drawable_gpu_data* packed = nullptr;
+    check(cadr_pack_buffers(_pack, &packed, nullptr, nullptr), "Renderer: pack buffers");
+    check(cadr_process_drawables(ctx, _storage->handleLevel(), reinterpret_cast<const void*>(_storage->handleTableDeviceAddress()),
+                                 packed, n, reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
+                                 reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
+          "Renderer: processDrawables");
 }
 
 }  // namespace CadR

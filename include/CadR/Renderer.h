@@ -125,6 +125,9 @@ public:
 
     size_t prepareRecording();
     void recordToCommandBuffer(std::vector<DrawCall>& out, size_t& drawableCounter);
+    // The same draw calls without the copy of the records (their packed
+    // array is on the device: Renderer::processDrawablesResident).
+    void recordDrawCalls(std::vector<DrawCall>& out, size_t& drawableCounter) const;
 
     std::vector<StateSet*> childList;
 
@@ -136,7 +139,9 @@ private:
     bool _forceRecording = false;
     std::vector<DrawableGpuData> _records;
     std::vector<Drawable*> _drawables;
+    std::vector<uint32_t> _slots;  // the records' slots in the renderer's device-resident pack
     friend class Drawable;
+    friend class Renderer;
 };
 
 // CadR::FrameInfo counterpart: GPU times of the last processed frame.
@@ -166,6 +171,13 @@ public:
     void recordSceneRendering(StateSet& root, std::vector<DrawCall>& out);
     void recordDrawableProcessing(size_t numDrawables, cadr_stream stream = nullptr);
     void processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream = nullptr);
+    // processDrawables() with the records device-resident (cadr_pack_*):
+    // instead of StateSet::recordToCommandBuffer's copy of every record into
+    // staging and its upload, a frame uploads only the records of drawables
+    // created since the previous frame, and lays the pack out again only when
+    // StateSet membership or list order changed.  Same draw calls, same
+    // indirect and DrawablePointers buffers as processDrawables().
+    void processDrawablesResident(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream = nullptr);
     void endFrame();
     size_t executeCopyOperations();
 
@@ -178,6 +190,19 @@ public:
 
 private:
     void growBuffers(size_t numDrawables);
+    uint32_t allocSlot(StateSet* owner, const DrawableGpuData& g);
+    void freeSlot(uint32_t slot) noexcept;
+    void growPack(uint32_t slots);
+    // Device-resident records: slot owner (nullptr = free), the records not
+    // yet on the device, whether the layout changed.
+    cadr_pack* _pack = nullptr;
+    uint32_t _packCapacity = 0;
+    std::vector<StateSet*> _slotOwner;
+    std::vector<uint32_t> _freeSlots;
+    std::vector<uint32_t> _newSlots;
+    std::vector<DrawableGpuData> _newRecords;
+    bool _layoutDirty = true;
+    friend class StateSet;
     std::unique_ptr<MemoryBackend> _ownBackend;
     MemoryBackend* _backend;
     cadr_context* _ownContext = nullptr;

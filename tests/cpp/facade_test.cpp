@@ -364,6 +364,73 @@ static void test_gpu()
                 r.dataStorage().handleLevel(), regs.size());
 }
 
+// Indirect commands and DrawablePointers of the last processed frame.
+static void download_frame(Renderer& r, size_t n, std::vector<cadr_draw_indirect_cmd>& ind,
+                           std::vector<cadr_drawable_pointers>& ptr)
+{
+    cadr_context* ctx = r.context();
+    check(cadr_context_synchronize(ctx), "sync");
+    ind.assign(n, cadr_draw_indirect_cmd{});
+    ptr.assign(n, cadr_drawable_pointers{});
+    check(cadr_download(ctx, ind.data(), reinterpret_cast<void*>(r.drawIndirectBufferAddress()), n * 16, nullptr), "dl");
+    check(cadr_download(ctx, ptr.data(), reinterpret_cast<void*>(r.drawablePointersBufferAddress()), n * 32, nullptr), "dl");
+    check(cadr_stream_synchronize(cadr_context_stream(ctx)), "sync");
+}
+
+static bool same_calls(const std::vector<DrawCall>& a, const std::vector<DrawCall>& b)
+{
+    if (a.size() != b.size()) return false;
+    for (size_t k = 0; k < a.size(); k++)
+        if (a[k].stateSet != b[k].stateSet || a[k].first != b[k].first || a[k].count != b[k].count ||
+            a[k].drawablePointers != b[k].drawablePointers || a[k].indirectOffset != b[k].indirectOffset)
+            return false;
+    return true;
+}
+
+// Device-resident recording against the copying path, frame by frame:
+// same draw calls, same buffers; new drawables and removals between frames;
+// a frame without changes launches nothing but processDrawables.
+static void test_gpu_resident()
+{
+    Renderer r(0);
+    SceneBuild S;
+    r.beginFrame();
+    build_scene(r, S, 120, 12000);
+    cadr_context* ctx = r.context();
+    for (int frame = 0; frame < 3 && !g_fail; frame++) {
+        if (frame == 1) {
+            // Removals (swap-removes reorder the lists) and new drawables.
+            for (size_t i = 3; i < S.drawables.size(); i += 11) S.drawables[i].destroy();
+            StateSet* sets[3] = {S.a.get(), S.b.get(), S.d.get()};
+            S.drawables.reserve(S.drawables.size() + 500);
+            for (int i = 0; i < 500; i++) {
+                auto ml = std::make_unique<MatrixList>(r);
+                ml->setMatrices(std::vector<Mat4>(1 + i % 2));
+                S.drawables.emplace_back(*S.geometries[i % S.geometries.size()], uint32_t(8 * (i % 3)), *ml, *sets[i % 3]);
+                S.lists.push_back(std::move(ml));
+            }
+        }
+        std::vector<DrawCall> host, res;
+        r.beginFrame();
+        r.processDrawables(*S.root, host);
+        size_t n = 0;
+        for (auto& c : host) n += c.count;
+        std::vector<cadr_draw_indirect_cmd> hi, ri;
+        std::vector<cadr_drawable_pointers> hp, rp;
+        download_frame(r, n, hi, hp);
+        const uint64_t l0 = cadr_context_launch_count(ctx);
+        r.processDrawablesResident(*S.root, res);
+        const uint64_t launches = cadr_context_launch_count(ctx) - l0;
+        download_frame(r, n, ri, rp);
+        EXPECT(same_calls(host, res), "frame %d: draw calls differ", frame);
+        EXPECT(std::memcmp(hi.data(), ri.data(), n * 16) == 0, "frame %d: indirect commands differ", frame);
+        EXPECT(std::memcmp(hp.data(), rp.data(), n * 32) == 0, "frame %d: drawable pointers differ", frame);
+        if (frame == 2) EXPECT(launches == 1, "an unchanged frame launched %llu kernels", (unsigned long long)launches);
+        check(cadr_context_check_device_error(ctx, nullptr), "device error");
+    }
+    std::printf("gpu resident: 3 frames equal to the copying path\n");
+}
+
 int main(int argc, char** argv)
 {
     const std::string mode = argc > 1 ? argv[1] : "cpu";
@@ -374,6 +441,7 @@ int main(int argc, char** argv)
             if (!g_fail) test_recording_and_oracle();
         } else {
             test_gpu();
+            if (!g_fail) test_gpu_resident();
         }
     } catch (const std::exception& e) {
         std::printf("FAIL: exception %s\n", e.what());

@@ -37,4 +37,5 @@ def test_facade_renderer_on_gpu(cuda_lib, oracle_lib, tmp_path):
     exe = _build(tmp_path)
     r = subprocess.run([str(exe), "gpu"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+    assert "gpu resident: 3 frames equal to the copying path" in r.stdout
     assert "facade gpu ok" in r.stdout
