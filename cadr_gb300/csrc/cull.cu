@@ -269,9 +269,7 @@ __global__ void __launch_bounds__(kScanThreads) leaf_tile_scan_kernel(uint32_t* 
 }
 
 constexpr uint32_t kWriteOffsetCap = 4096;  // StateSet offsets staged in shared memory
-#ifndef CADR_WRITE_CTAS_PER_SM
-#define CADR_WRITE_CTAS_PER_SM 6
-#endif
+constexpr int kWriteCtasPerSm = 6;  // 40 registers; 5 and 8 measured slower
 
 // Plain pass, launch 3 of 3: one CTA per tile writes the commands and
 // counts from the planes and the tile's carry.  No CTA waits for another.
@@ -280,7 +278,7 @@ constexpr uint32_t kWriteOffsetCap = 4096;  // StateSet offsets staged in shared
 // gathers) is loaded while the scan still runs, and only the carry is read
 // after griddepcontrol.wait.  The loads are independent of one another,
 // so a tile costs about two memory round trips.
-__global__ void __launch_bounds__(kLeafThreads, CADR_WRITE_CTAS_PER_SM) leaf_write_kernel(const LeafArgs a)
+__global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kernel(const LeafArgs a)
 {
     __shared__ LeafTile::Smem sm;
     extern __shared__ uint32_t s_off[];
