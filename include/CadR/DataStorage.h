@@ -56,7 +56,8 @@ private:
 };
 
 // Host memory standing in for device memory: one arena whose host addresses
-// are the "device" addresses, so a CPU checker can follow every pointer.
+// are the "device" addresses, so host code (the oracle) can follow every
+// pointer.
 class HostMemoryBackend : public MemoryBackend {
 public:
     explicit HostMemoryBackend(size_t arenaBytes = size_t(256) << 20);

@@ -1,8 +1,8 @@
 /*
  * cadr_oracle.c - CPU oracle of the drawable-processing pass.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
- * baseline.  See cadr_oracle.h for what each function restates.  Must be
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA path is compared against and
+ * the timed CPU baseline.  See cadr_oracle.h for what each function restates.  Must be
  * compiled with -ffp-contract=off (oracle/Makefile does).
  */
 #include "cadr_oracle.h"

@@ -1,7 +1,7 @@
 /*
  * cadr_oracle.h - CPU oracle of the drawable-processing pass.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the CUDA path is
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA path is
  * compared against (tests/, __graft_entry__.smoke) and the CPU baseline that
  * bench.py times.  The product path (libcadr_cuda.so) never links or calls it.
  *
