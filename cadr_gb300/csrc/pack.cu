@@ -50,22 +50,41 @@ constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr int kPackThreads = 256;
 
 // Per-StateSet drawable counts and the depth-first rank of every StateSet
-// (rank[dfs[j]] = j; a repeated StateSet id in dfs is an error).
-__global__ void pack_count_kernel(const uint32_t* __restrict__ set_of_slot, uint32_t n, uint32_t S,
-                                  const uint32_t* __restrict__ dfs, uint32_t* __restrict__ rank,
-                                  uint32_t* __restrict__ count, uint32_t* error)
+// (rank[dfs[j]] = j; a repeated StateSet id in dfs is an error).  With at
+// most kSmemBins StateSets each CTA counts into shared memory and adds its
+// non-zero bins once: a few StateSets holding millions of drawables would
+// otherwise serialise on a few global counters.
+constexpr uint32_t kSmemBins = 4096;
+
+__global__ void __launch_bounds__(kPackThreads) pack_count_kernel(const uint32_t* __restrict__ set_of_slot, uint32_t n,
+                                                                  uint32_t S, const uint32_t* __restrict__ dfs,
+                                                                  uint32_t* __restrict__ rank,
+                                                                  uint32_t* __restrict__ count, uint32_t* error)
 {
+    __shared__ uint32_t bins[kSmemBins];
+    const bool local = S <= kSmemBins;
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local) {
+        for (uint32_t b = threadIdx.x; b < S; b += blockDim.x) bins[b] = 0;
+        __syncthreads();
+    }
     if (k < S) {
         const uint32_t s = dfs[k];
         if (s >= S || atomicExch(&rank[s], k) != kNoSlot) atomicOr(error, CADR_DEVERR_BAD_INDEX);
     }
     if (k < n) {
         const uint32_t s = set_of_slot[k];
-        if (s < S)
-            atomicAdd(&count[s], 1u);
-        else
+        if (s >= S)
             atomicOr(error, CADR_DEVERR_BAD_INDEX);
+        else if (local)
+            atomicAdd(&bins[s], 1u);
+        else
+            atomicAdd(&count[s], 1u);
+    }
+    if (local) {
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < S; b += blockDim.x)
+            if (bins[b]) atomicAdd(&count[b], bins[b]);
     }
 }
 
