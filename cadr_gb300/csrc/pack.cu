@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "capi_internal.h"
+#include "handles.cuh"
 
 using namespace cadr;
 
@@ -187,6 +188,33 @@ __global__ void pack_patch_kernel(const uint32_t* __restrict__ slots, const uint
     pool[3ull * k + part] = r;
     const uint32_t p = __ldg(pos_of_slot + k);
     if (p != kNoSlot) packed[3ull * p + part] = r;
+}
+
+// Tier A straight from the pool: slot k's record is resolved and its
+// indirect command and pointers are written at its packed position, for
+// the positions below n_draw.  Slots come in the order their drawables
+// were created, which is also the order of their MatrixList and
+// drawable-data handles, so the handle-table reads of a warp fall on
+// neighbouring entries; the outputs are scattered instead.  A slot outside
+// the drawn positions is not read at all.
+template <int LEVEL>
+__global__ void __launch_bounds__(256) pack_process_kernel(const uint64_t* __restrict__ root,
+                                                           const ulonglong2* __restrict__ pool,
+                                                           const uint32_t* __restrict__ pos_of_slot, uint32_t n,
+                                                           uint32_t n_draw, uint4* __restrict__ indirect,
+                                                           ulonglong2* __restrict__ pointers)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t p = __ldg(pos_of_slot + k);
+    if (p >= n_draw) return;  // also kNoSlot
+    const ulonglong2* d = pool + 3ull * k;
+    uint4 ind;
+    ulonglong2 p0, p1;
+    resolve_record<LEVEL>(root, __ldg(d), __ldg(d + 1), __ldg(d + 2), ind, p0, p1);
+    indirect[p] = ind;
+    pointers[2ull * p] = p0;
+    pointers[2ull * p + 1] = p1;
 }
 
 uint32_t blocks(uint64_t items) { return (uint32_t)((items + kPackThreads - 1) / kPackThreads); }
@@ -356,6 +384,38 @@ CADR_API cadr_status cadr_pack_patch(cadr_pack* pk, const uint32_t* slots, const
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "pack_patch: launch");
     ctx->launches++;
+    return CADR_OK;
+}
+
+CADR_API cadr_status cadr_pack_process_drawables(cadr_pack* pk, uint32_t handle_level, const void* handle_table,
+                                                 uint32_t num_draw_records, cadr_draw_indirect_cmd* indirect,
+                                                 cadr_drawable_pointers* pointers, cadr_stream stream)
+{
+    if (!pk || (num_draw_records && (!handle_table || !indirect || !pointers)))
+        return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: null argument");
+    if (handle_level < 1 || handle_level > 3)
+        return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: handle level %u", handle_level);
+    if (num_draw_records > pk->num_slots)
+        return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: %u records drawn, %u in the layout",
+                    num_draw_records, pk->num_slots);
+    if ((reinterpret_cast<uintptr_t>(handle_table) | reinterpret_cast<uintptr_t>(indirect) |
+         reinterpret_cast<uintptr_t>(pointers)) % 16)
+        return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: misaligned buffer");
+    if (num_draw_records == 0) return CADR_OK;
+    cudaStream_t s = pick_stream(pk->ctx, stream);
+    auto root = static_cast<const uint64_t*>(handle_table);
+    auto pool = reinterpret_cast<const ulonglong2*>(pk->pool);
+    auto ind = reinterpret_cast<uint4*>(indirect);
+    auto ptr = reinterpret_cast<ulonglong2*>(pointers);
+    const uint32_t grid = blocks(pk->num_slots);
+    switch (handle_level) {
+    case 1: pack_process_kernel<1><<<grid, 256, 0, s>>>(root, pool, pk->pos_of_slot, pk->num_slots, num_draw_records, ind, ptr); break;
+    case 2: pack_process_kernel<2><<<grid, 256, 0, s>>>(root, pool, pk->pos_of_slot, pk->num_slots, num_draw_records, ind, ptr); break;
+    default: pack_process_kernel<3><<<grid, 256, 0, s>>>(root, pool, pk->pos_of_slot, pk->num_slots, num_draw_records, ind, ptr); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "pack_process_drawables: launch");
+    pk->ctx->launches++;
     return CADR_OK;
 }
 

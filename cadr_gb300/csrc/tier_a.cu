@@ -12,29 +12,12 @@
 // with the same 32-bit truncations.  The 48-byte record is read as three
 // 16-byte vectors; the five lookups are independent chains, so their loads
 // overlap; the 16- and 32-byte outputs are written as 16-byte vectors.
+#include "handles.cuh"
 #include "kernels.cuh"
 
 namespace cadr {
 
 namespace {
-
-__device__ __forceinline__ uint64_t ld_u64(uint64_t addr)
-{
-    return __ldg(reinterpret_cast<const unsigned long long*>(addr));
-}
-
-template <int LEVEL>
-__device__ __forceinline__ uint64_t lookup(const uint64_t* __restrict__ root, uint64_t h)
-{
-    if (LEVEL == 1) return __ldg(reinterpret_cast<const unsigned long long*>(root) + (uint32_t)h);
-    if (LEVEL == 2) {
-        const uint64_t t2 = __ldg(reinterpret_cast<const unsigned long long*>(root) + (uint32_t)(h >> 11));
-        return ld_u64(t2 + 8ull * ((uint32_t)h & 0x7ffu));
-    }
-    const uint64_t t2 = __ldg(reinterpret_cast<const unsigned long long*>(root) + (uint32_t)(h >> 22));
-    const uint64_t t3 = ld_u64(t2 + 8ull * ((uint32_t)(h >> 11) & 0x7ffu));
-    return ld_u64(t3 + 8ull * ((uint32_t)h & 0x7ffu));
-}
 
 template <int LEVEL>
 __global__ void __launch_bounds__(256) process_drawables_kernel(
@@ -47,24 +30,12 @@ __global__ void __launch_bounds__(256) process_drawables_kernel(
     const ulonglong2 d0 = __ldg(d + 0);  // vertexDataHandle, indexDataHandle
     const ulonglong2 d1 = __ldg(d + 1);  // matrixListHandle, drawableDataHandle
     const ulonglong2 d2 = __ldg(d + 2);  // primitiveSetHandle, primitiveSetOffset | padding
-    const uint64_t ps = lookup<LEVEL>(root, d2.x) + (uint64_t)(uint32_t)d2.y;
-    const uint64_t ml = lookup<LEVEL>(root, d1.x);
-    const uint64_t vtx = lookup<LEVEL>(root, d0.x);
-    const uint64_t idx = lookup<LEVEL>(root, d0.y);
-    const uint64_t dd = lookup<LEVEL>(root, d1.y);
-    uint32_t count, first;
-    if ((ps & 7u) == 0) {
-        const uint2 v = __ldg(reinterpret_cast<const uint2*>(ps));
-        count = v.x;
-        first = v.y;
-    } else {
-        count = __ldg(reinterpret_cast<const unsigned int*>(ps));
-        first = __ldg(reinterpret_cast<const unsigned int*>(ps + 4));
-    }
-    const uint32_t num_matrices = __ldg(reinterpret_cast<const unsigned int*>(ml));
-    indirect[i] = make_uint4(count, num_matrices, first, 0u);
-    pointers[i * 2 + 0] = make_ulonglong2(vtx, idx);
-    pointers[i * 2 + 1] = make_ulonglong2(ml, dd);
+    uint4 ind;
+    ulonglong2 p0, p1;
+    resolve_record<LEVEL>(root, d0, d1, d2, ind, p0, p1);
+    indirect[i] = ind;
+    pointers[i * 2 + 0] = p0;
+    pointers[i * 2 + 1] = p1;
 }
 
 }  // namespace

@@ -349,16 +349,14 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
         _newSlots.clear();
         _newRecords.clear();
     }
-    if (_layoutDirty) {
-        check(cadr_pack_repack(_pack, stream), "Renderer: repack");
-        _layoutDirty = false;
-    }
+    _layoutDirty = false;
     if (n == 0) return;
-    const cadr_drawable_gpu_data* packed = nullptr;
-    check(cadr_pack_buffers(_pack, &packed, nullptr, nullptr), "Renderer: pack buffers");
-    check(cadr_process_drawables(ctx, _storage->handleLevel(), reinterpret_cast<const void*>(_storage->handleTableDeviceAddress()),
-                                 packed, n, reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
-                                 reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
+    // processDrawables straight from the pool (slots in creation order), so
+    // no repack is needed; the first n packed positions are the drawn ones.
+    check(cadr_pack_process_drawables(_pack, _storage->handleLevel(),
+                                      reinterpret_cast<const void*>(_storage->handleTableDeviceAddress()), uint32_t(n),
+                                      reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
+                                      reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
           "Renderer: processDrawables");
 }
 

@@ -140,6 +140,7 @@ _SIGS = {
     "cadr_pack_repack": ([vp, vp], i32),
     "cadr_pack_patch": ([vp, vp, vp, u32, vp], i32),
     "cadr_pack_buffers": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(u32)], i32),
+    "cadr_pack_process_drawables": ([vp, u32, vp, u32, vp, vp, vp], i32),
     "cadr_check_draws": ([vp, vp, vp, u64, C.POINTER(MemoryRegion), u32, C.POINTER(ConsumerView), vp, vp], i32),
     "cadr_server_create": ([vp, C.POINTER(ServerConfig), C.POINTER(vp)], i32),
     "cadr_server_destroy": ([vp], i32),
@@ -476,6 +477,10 @@ class Pack:
         r = np.ascontiguousarray(records)
         assert r.dtype.itemsize == 48 and len(r) == len(sl)
         check(self.lib.cadr_pack_patch(self.handle, _ptr(sl), _ptr(r), len(sl), stream))
+
+    def process_drawables(self, level: int, root: int, n_draw: int, indirect, pointers, stream=None):
+        check(self.lib.cadr_pack_process_drawables(self.handle, level, root, n_draw, _ptr(indirect),
+                                                   _ptr(pointers), stream))
 
     def buffers(self):
         packed, offsets, n = vp(), vp(), u32()

@@ -248,6 +248,18 @@ CADR_API cadr_status cadr_pack_repack(cadr_pack* pack, cadr_stream stream);
 /* records[k] replaces slot slots[k], in the pool and in the packed array. */
 CADR_API cadr_status cadr_pack_patch(cadr_pack* pack, const uint32_t* slots, const cadr_drawable_gpu_data* records,
                                      uint32_t count, cadr_stream stream);
+/* cadr_process_drawables over the packed records [0, num_draw_records),
+ * read from the pool instead of the packed array: each slot's record is
+ * resolved in slot order and its indirect command and DrawablePointers are
+ * written at its packed position.  The output equals cadr_process_drawables
+ * on the packed array (after a repack) for those positions; no repack is
+ * needed.  Slots whose packed position is num_draw_records or more are not
+ * read, so they may hold any bytes (free slots).  With slots handed out in
+ * drawable creation order, the handle-table reads of neighbouring slots
+ * are neighbours too. */
+CADR_API cadr_status cadr_pack_process_drawables(cadr_pack* pack, uint32_t handle_level, const void* handle_table,
+                                                 uint32_t num_draw_records, cadr_draw_indirect_cmd* indirect,
+                                                 cadr_drawable_pointers* pointers, cadr_stream stream);
 /* Device pointers: the packed records (num_slots of them) and the region
  * offsets (num_state_sets + 1): StateSet dfs_order[j] occupies packed
  * records [offsets[j], offsets[j+1]), which is the reference's

@@ -140,3 +140,57 @@ def test_tier_a_on_packed_records(ctx):
     assert np.array_equal(ctx.download(ind, np.uint32, (n, 4)), r_ind)
     assert np.array_equal(ctx.download(ptr, np.uint64, (n, 4)), r_ptr)
     assert np.array_equal(ctx.download(offsets, np.uint32, (len(dfs) + 1,)), starts)
+
+
+def creation_order_layout(im, G):
+    """Slots in drawable creation order (the order of the MatrixList
+    handles, 1 + 3G + i), StateSet j = packed region j."""
+    n = im.drawables.shape[0]
+    starts = np.concatenate([[0], np.cumsum(im.state_set_counts)]).astype(np.int64)
+    region = np.repeat(np.arange(len(im.state_set_counts)), im.state_set_counts)
+    slot_of_pos = (im.drawables["matrix_list_handle"].astype(np.int64) - 1 - 3 * G)
+    ss = np.empty(n, np.uint32)
+    li = np.empty(n, np.uint32)
+    ss[slot_of_pos] = region
+    li[slot_of_pos] = np.arange(n) - starts[region]
+    pool = np.empty_like(im.drawables)
+    pool[slot_of_pos] = im.drawables
+    return np.arange(len(im.state_set_counts), dtype=np.uint32), ss, li, pool
+
+
+@pytest.mark.parametrize("level_n", [3000, 300_000, 5_000_000])
+def test_process_from_pool_equals_packed(ctx, level_n):
+    """cadr_pack_process_drawables (records read in slot order, outputs
+    scattered to their packed positions) equals processDrawables over the
+    packed array; extra slots laid out after the drawn positions are not
+    touched."""
+    G = 4096 if level_n > 3000 else None
+    kw = dict(n=level_n, num_state_sets=12, num_geometries=G or min(level_n, 4096))
+    probe = tier_a.build(seed=41, base=1 << 40, **kw)
+    buf = ctx.alloc(probe.image.nbytes + 4096)
+    im = tier_a.build(seed=41, base=buf.ptr, **kw)
+    r_ind, r_ptr = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables,
+                                          threads=bind.max_threads())
+    ctx.upload(buf, im.image)
+    n = im.drawables.shape[0]
+    dfs, ss, li, pool = creation_order_layout(im, kw["num_geometries"])
+    # 1,000 more slots in a trailing StateSet that is not drawn (valid
+    # records, so that reading them would be harmless but visible).
+    extra = 1000
+    dfs = np.append(dfs, len(dfs)).astype(np.uint32)
+    ss = np.concatenate([ss, np.full(extra, len(dfs) - 1, np.uint32)])
+    li = np.concatenate([li, np.arange(extra, dtype=np.uint32)])
+    pool = np.concatenate([pool, im.drawables[:extra]])
+    pk = lib.Pack(ctx, n + extra)
+    pk.set_layout(dfs, ss, li)
+    pk.upload(pool)
+    ind, ptr = ctx.alloc((n + extra) * 16), ctx.alloc((n + extra) * 32)
+    ctx.upload(ind, np.full((n + extra) * 4, 0xDEADBEEF, np.uint32))
+    ctx.upload(ptr, np.full((n + extra) * 4, 0xDEADBEEFDEADBEEF, np.uint64))
+    pk.process_drawables(im.level, im.root, n, ind, ptr)
+    ctx.sync()
+    assert ctx.check_device_error() == 0
+    g_ind = ctx.download(ind, np.uint32, (n + extra, 4))
+    g_ptr = ctx.download(ptr, np.uint64, (n + extra, 4))
+    assert np.array_equal(g_ind[:n], r_ind) and np.array_equal(g_ptr[:n], r_ptr)
+    assert (g_ind[n:] == 0xDEADBEEF).all() and (g_ptr[n:] == 0xDEADBEEFDEADBEEF).all()
