@@ -20,13 +20,13 @@ namespace cadr {
 
 namespace {
 
+// A 64-byte matrix record in two 256-bit loads (records are 32-byte
+// aligned: every array sits at a 256-byte offset of the scene arena).
 __device__ __forceinline__ void load_mat(const float4* __restrict__ p, float4& c0, float4& c1,
                                          float4& c2, float4& c3)
 {
-    c0 = ld_nc_f4(p + 0);
-    c1 = ld_nc_f4(p + 1);
-    c2 = ld_nc_f4(p + 2);
-    c3 = ld_nc_f4(p + 3);
+    ld_nc_f8(p, c0, c1);
+    ld_nc_f8(p + 2, c2, c3);
 }
 
 using LeafTile = Tile<kLeafThreads, kLeafIpt>;
@@ -55,6 +55,17 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint3
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t words = (uint32_t)leaf_plane_stride(a.n);
+    // The parent indices of all rows are loaded first, so that each row's
+    // parent-matrix gather leaves with its own loads instead of one memory
+    // round trip after them.
+    uint32_t par[kLeafIpt];
+    if (a.parent) {
+#pragma unroll
+        for (int j = 0; j < kLeafIpt; j++) {
+            const uint32_t i = b + (uint32_t)(j * kLeafThreads + t);
+            par[j] = i < a.n ? ld_nc_u32(a.parent + i) : 0u;
+        }
+    }
 #pragma unroll
     for (int j = 0; j < kLeafIpt; j++) {
         const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
@@ -69,13 +80,13 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint3
                 load_mat(a.local + (size_t)i * 4, l0, l1, l2, l3);
                 const float4 sp = ld_nc_f4(a.sphere + i);
                 if (a.parent) {
-                    uint32_t p = ld_nc_u32(a.parent + i);
+                    uint32_t p = par[j];
                     if (p >= a.num_parents) {
                         atomicOr(a.error, CADR_DEVERR_BAD_INDEX);
                         p = 0;
                     }
-                    const float4* pp = a.parent_world + (size_t)p * 4;
-                    const float4 p0 = __ldg(pp), p1 = __ldg(pp + 1), p2 = __ldg(pp + 2), p3 = __ldg(pp + 3);
+                    float4 p0, p1, p2, p3;
+                    load_mat(a.parent_world + (size_t)p * 4, p0, p1, p2, p3);
                     w0 = mat_col(p0, p1, p2, p3, l0);
                     w1 = mat_col(p0, p1, p2, p3, l1);
                     w2 = mat_col(p0, p1, p2, p3, l2);
@@ -375,11 +386,11 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
     }
     float4 l0, l1, l2, l3;
     load_mat(local + (size_t)i * 4, l0, l1, l2, l3);
+    // Default-cached stores: the next level (or the leaf pass) gathers
+    // these matrices as parents while they are still in L2.
     float4* wp = world + (size_t)i * 4;
-    wp[0] = mat_col(p0, p1, p2, p3, l0);
-    wp[1] = mat_col(p0, p1, p2, p3, l1);
-    wp[2] = mat_col(p0, p1, p2, p3, l2);
-    wp[3] = mat_col(p0, p1, p2, p3, l3);
+    st_f8(wp, mat_col(p0, p1, p2, p3, l0), mat_col(p0, p1, p2, p3, l1));
+    st_f8(wp + 2, mat_col(p0, p1, p2, p3, l2), mat_col(p0, p1, p2, p3, l3));
 }
 
 }  // namespace
