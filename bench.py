@@ -759,6 +759,9 @@ def main():
         for s in range(sc.num_state_sets)))
     clk = clocks.stop()
     e2e_value = world * sc.n / e2e_s / 1e9
+    # The same traffic without the arithmetic, after the timed regions: the
+    # bandwidth the stream kernel's access pattern can reach on this GPU.
+    probe_gbs = ctx.measure_stream_mix(sc.n, 20)
 
     value = world * sc.n / (ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
@@ -779,7 +782,9 @@ def main():
                      "traffic": committed_traffic("stream_kernel_traffic_bytes"),
                      "kernel": "leaf_stream_kernel (world matrices, spheres, cull, LOD; bit-planes)",
                      "algorithmic_bytes_per_launch": stream_bytes, "launch_ms": stream_ms,
-                     "peak_source": f"{peak_kind} hbm_gbs"},
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "same_traffic_probe_gbs": probe_gbs,
+                     "frac_of_probe": (achieved / probe_gbs) if achieved and probe_gbs else None},
         "leaf_stage": {"kernels": "leaf_stream_kernel + leaf_tile_scan_kernel + leaf_write_kernel",
                        "achieved": achieved_stage, "unit": "GB/s",
                        "frac": (achieved_stage / peak) if achieved_stage else None,

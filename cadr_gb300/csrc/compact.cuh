@@ -220,25 +220,28 @@ struct Tile {
     {
         uint4 ent[IPT];
         gather(vis_bits, lod_bits, geo, lods, G, L, error, ent);
-        write_ent(sm, vis_bits, ent, b, n, first_tile, offsets, S, cmds, counts);
+        write_ent(sm, vis_bits, ent, b, n, first_tile, offsets, S, cmds, counts, error);
     }
 
     // write() with the LOD entries already gathered.
     __device__ static __forceinline__ void write_ent(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[IPT],
                                                      uint32_t b, uint32_t n, bool first_tile,
                                                      const uint32_t* __restrict__ offsets, uint32_t S,
-                                                     uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts)
+                                                     uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts,
+                                                     uint32_t* error)
     {
-        write_cmds<0, IPT>(sm, vis_bits, ent, b, offsets, cmds);
+        write_cmds<0, IPT>(sm, vis_bits, ent, b, n, offsets, cmds, error);
         write_counts(sm, b, n, first_tile, offsets, S, counts);
     }
 
     // The commands of the thread's visible items in rows [J0, J1); bit j of
-    // vis_bits and ent[j - J0] belong to row j.
+    // vis_bits and ent[j - J0] belong to row j.  A slot outside the n
+    // commands (only possible from inconsistent offsets or carries) is
+    // flagged with CADR_DEVERR_BAD_INDEX and not written.
     template <int J0, int J1>
     __device__ static __forceinline__ void write_cmds(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[J1 - J0],
-                                                      uint32_t b, const uint32_t* __restrict__ offsets,
-                                                      uint32_t* __restrict__ cmds)
+                                                      uint32_t b, uint32_t n, const uint32_t* __restrict__ offsets,
+                                                      uint32_t* __restrict__ cmds, uint32_t* error)
     {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
@@ -251,6 +254,10 @@ struct Tile {
             const uint32_t start = (r == rf) ? start_f : offsets[r];
             const uint32_t ei = excl(sm, i - b);
             const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
+            if (slot >= n) {
+                atomicOr(error, CADR_DEVERR_BAD_INDEX);
+                continue;
+            }
             const uint4 e = ent[j - J0];
             uint32_t* c = cmds + (size_t)slot * 5;
             c[0] = e.x;

@@ -156,13 +156,9 @@ __global__ void __launch_bounds__(kLeafThreads, 4) leaf_stream_kernel(const Leaf
     __shared__ uint32_t s_last_start;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t tile = blockIdx.x, b = tile * (uint32_t)kLeafTile;
-    if (t == 0) {
-        // Start of the region holding the tile's last drawable; its search
-        // overlaps the stream.
-        const uint32_t e = min(b + (uint32_t)kLeafTile, a.n);
-        const uint32_t rl = min(region_of(a.offsets, 0, a.num_state_sets + 1, e - 1), a.num_state_sets - 1);
-        s_last_start = a.offsets[rl];
-    }
+    // Start of the region holding the tile's last drawable (from the
+    // scene's per-tile table); the load overlaps the stream.
+    if (t == 0) s_last_start = __ldg(a.tile_start + tile);
     stream_tile<true>(a, b, ballot, xb[warp]);
     __syncthreads();
     if (warp == 0) {
@@ -320,7 +316,7 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     if (t == 0) sm.info[2] = load_relaxed_u32(a.tile_words + tile);
     __syncthreads();
     LeafTile::scan(sm, off, a.num_state_sets, b, a.n);
-    LeafTile::write_ent(sm, vis_bits, ent, b, a.n, tile == 0, off, a.num_state_sets, a.cmds, a.counts);
+    LeafTile::write_ent(sm, vis_bits, ent, b, a.n, tile == 0, off, a.num_state_sets, a.cmds, a.counts, a.error);
 }
 
 // Internal level propagation.  With `staged`, the CTA's run of parents

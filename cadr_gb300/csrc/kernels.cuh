@@ -26,6 +26,7 @@ struct LeafArgs {
     const float4* sphere;         // N
     const uint32_t* geometry;     // N
     const uint32_t* offsets;      // S + 1
+    const uint32_t* tile_start;   // per leaf tile: start of the region holding its last drawable
     uint32_t num_state_sets;
     const uint4* lods;            // G * L
     uint32_t num_geometries;

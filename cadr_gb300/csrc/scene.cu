@@ -20,6 +20,35 @@ ViewConst to_view_const(const cadr_view& v)
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+static cadr_status before_upload(cadr_scene* sc);
+static cadr_status after_upload(cadr_scene* sc);
+
+// The plain pass's per-tile table: for each leaf tile of kLeafTile
+// drawables, the start of the StateSet region holding its last drawable
+// (the region search the stream kernel would otherwise do per CTA).  Built
+// on the host from the validated offsets at every commit, uploaded on the
+// upload stream.
+static cadr_status upload_tile_starts(cadr_scene* sc)
+{
+    const uint64_t N = sc->desc.num_drawables;
+    const uint32_t S = sc->desc.num_state_sets;
+    const std::vector<uint32_t>& off = sc->h_offsets;
+    const uint64_t tiles = (N + kLeafTile - 1) / kLeafTile;
+    sc->h_tile_start.resize(tiles);
+    for (uint64_t t = 0; t < tiles; t++) {
+        const uint32_t last = (uint32_t)(std::min<uint64_t>((t + 1) * kLeafTile, N) - 1);
+        size_t r = (size_t)(std::upper_bound(off.begin(), off.end(), last) - off.begin()) - 1;
+        if (r > S - 1) r = S - 1;
+        sc->h_tile_start[t] = off[r];
+    }
+    if (tiles == 0) return CADR_OK;
+    cadr_status st = before_upload(sc);
+    if (st == CADR_OK)
+        st = upload_bytes(sc->ctx, sc->tile_start, sc->h_tile_start.data(), tiles * 4, sc->ctx->upload_stream);
+    if (st != CADR_OK) return st;
+    return after_upload(sc);
+}
+
 static cadr_status commit(cadr_scene* sc)
 {
     const uint32_t S = sc->desc.num_state_sets;
@@ -34,6 +63,8 @@ static cadr_status commit(cadr_scene* sc)
     for (uint32_t s = 0; s < S; s++)
         if (off[s + 1] < off[s]) return fail(CADR_ERR_INVALID_ARG, "scene_commit: StateSet offsets not sorted at %u", s);
     sc->h_offsets = std::move(off);
+    cadr_status st = upload_tile_starts(sc);
+    if (st != CADR_OK) return st;
     sc->committed = true;
     return CADR_OK;
 }
@@ -104,6 +135,7 @@ LeafArgs leaf_args(cadr_scene* sc)
     a.sphere = reinterpret_cast<const float4*>(sc->buf.sphere);
     a.geometry = sc->buf.geometry;
     a.offsets = sc->buf.state_set_offsets;
+    a.tile_start = sc->tile_start;
     a.num_state_sets = d.num_state_sets;
     a.lods = reinterpret_cast<const uint4*>(sc->buf.lods);
     a.num_geometries = d.num_geometries;
@@ -149,6 +181,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     const size_t o_lods = off; off = align256(off + (size_t)d.num_geometries * d.num_lods * 16);
     const size_t o_world = off; off = align256(off + N * 64);
     const size_t o_wsph = off; off = align256(off + N * 16);
+    const size_t o_tiles = off; off = align256(off + (N + kLeafTile - 1) / kLeafTile * 4);
 
     auto* sc = new cadr_scene();
     sc->ctx = ctx;
@@ -176,6 +209,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     sc->buf.lods = reinterpret_cast<cadr_lod*>(base + o_lods);
     sc->buf.world = reinterpret_cast<float*>(base + o_world);
     sc->buf.world_sphere = reinterpret_cast<float*>(base + o_wsph);
+    sc->tile_start = reinterpret_cast<uint32_t*>(base + o_tiles);
     // Defaults: all drawables in StateSet 0 until offsets are uploaded.
     std::vector<uint32_t> off0(d.num_state_sets + 1, (uint32_t)N);
     off0[0] = 0;

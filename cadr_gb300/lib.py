@@ -105,6 +105,7 @@ _SIGS = {
     "cadr_context_set_spin_limit_ns": ([vp, u64], i32),
     "cadr_context_synchronize": ([vp], i32),
     "cadr_context_launch_count": ([vp], u64),
+    "cadr_measure_stream_mix": ([vp, u64, u32, C.POINTER(C.c_double)], i32),
     "cadr_context_check_device_error": ([vp, C.POINTER(u32)], i32),
     "cadr_debug_set_fault": ([vp, u32], i32),
     "cadr_context_set_collect_frame_info": ([vp, i32], i32),
@@ -299,6 +300,12 @@ class Context:
             out += [(buf[i].propagate_ms, buf[i].leaf_ms, buf[i].total_ms, buf[i].stream_ms) for i in range(n.value)]
             if n.value < 256:
                 return out
+
+    def measure_stream_mix(self, n: int, reps: int = 20) -> float:
+        """GB/s of the leaf stream's traffic without its arithmetic."""
+        g = C.c_double()
+        check(self.lib.cadr_measure_stream_mix(self.handle, n, reps, C.byref(g)))
+        return g.value
 
     @property
     def launch_count(self) -> int:

@@ -177,6 +177,14 @@ CADR_API cadr_status cadr_context_set_spin_limit_ns(cadr_context* ctx, uint64_t 
 CADR_API cadr_status cadr_context_synchronize(cadr_context* ctx);
 /* Number of kernels this library launched through ctx since creation. */
 CADR_API uint64_t cadr_context_launch_count(cadr_context* ctx);
+/* Measurement aid (no reference counterpart): the HBM bandwidth, in GB/s,
+ * of a kernel that moves the plain pass's leaf-stream traffic for
+ * `num_drawables` drawables (64 B local + 16 B sphere + 4 B parent index
+ * read, 64 B world matrix written per drawable, the stream kernel's access
+ * pattern) without its arithmetic, timed over `reps` launches on the
+ * context stream.  Allocates and frees 148 B per drawable. */
+CADR_API cadr_status cadr_measure_stream_mix(cadr_context* ctx, uint64_t num_drawables, uint32_t reps,
+                                             double* gbytes_per_s);
 
 /* Device memory helpers (stream-ordered pool of the context's device). */
 CADR_API cadr_status cadr_device_alloc(cadr_context* ctx, size_t bytes, void** out);
