@@ -757,6 +757,17 @@ def main():
         np.array_equal(got_cmds[int(offs[s]):int(offs[s]) + int(got_counts[s])],
                        ref_cmds[int(offs[s]):int(offs[s]) + int(got_counts[s])])
         for s in range(sc.num_state_sets)))
+    # The host link's own bound on a step: the same uploads alone, back to
+    # back (no pass, no read-back), after the e2e measurement.
+    up_stream = L.cadr_context_upload_stream(ctx.handle)
+    for k in range(2):
+        e2e_upload(k)
+    lib.check(L.cadr_stream_synchronize(up_stream))
+    t2 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_upload(k)
+    lib.check(L.cadr_stream_synchronize(up_stream))
+    upload_only_s = (time.perf_counter() - t2) / e2e_steps
     clk = clocks.stop()
     e2e_value = world * sc.n / e2e_s / 1e9
     # The same traffic without the arithmetic, after the timed regions: the
@@ -795,6 +806,8 @@ def main():
                  "step_gbs": step_algorithmic_bytes(sc, visible) / (ms / 1e3) / 1e9},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h_total // max(1, e2e_steps), "ms_per_step": e2e_s * 1e3,
+                "upload_only_ms_per_step": upload_only_s * 1e3,
+                "host_link_h2d_gbs": h2d / upload_only_s / 1e9,
                 "pipelining": "two device scenes alternate; a step's uploads overlap the previous step's pass and read-back",
                 "readback_equals_device_pass": e2e_same},
         "gpu_launches": launches,

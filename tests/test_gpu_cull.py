@@ -186,3 +186,12 @@ def test_bad_parent_index_is_reported(ctx):
     # the context stays usable
     res, _, _ = gpu_cull(ctx, scenes.small_scene(seed=3, n=5000, num_levels=2, num_state_sets=3))
     assert res["counts"].sum() > 0
+
+
+def test_stream_mix_probe_measures_bandwidth(ctx):
+    """cadr_measure_stream_mix (the bench's same-traffic ceiling) runs and
+    returns a bandwidth, and rejects an empty size."""
+    gbs = ctx.measure_stream_mix(1 << 22, 3)
+    assert 100.0 < gbs < 20_000.0
+    with pytest.raises(lib.CadrError):
+        ctx.measure_stream_mix(0, 3)
