@@ -52,7 +52,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (default: min(steps, 50))")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form (C4) measurement")
-    ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a"])
+    ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a", "batched"])
+    ap.add_argument("--batched-tuning", default="", help="batched: block_threads,items_per_thread,ctas_per_sm "
+                                                           "instead of the autotuner's pick")
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of request stream")
     ap.add_argument("--serving-scenes", type=int, default=64)
@@ -166,7 +168,7 @@ def step_algorithmic_bytes(sc, visible: int) -> int:
     return b
 
 
-def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32):
+def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_override: str = ""):
     """Batched form on C4: 256 views (8 per scene) over 32 scenes of
     1,000 .. 2,000,000 drawables, culled by one persistent launch replayed
     from a captured CUDA graph with the autotuned shape, against 256
@@ -185,7 +187,12 @@ def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32):
             items.append((ds, v, lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False)))
             plain_outs.append(lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False))
     arr = lib.batch_views(items)
-    tuning, tune_ms = lib.autotune_batched(ctx, arr, reps=3)
+    if tuning_override:
+        bt, ipt, cps = (int(x) for x in tuning_override.split(","))
+        ctx.set_tuning(bt, ipt, cps)
+        tuning, tune_ms = ctx.get_tuning(), None
+    else:
+        tuning, tune_ms = lib.autotune_batched(ctx, arr, reps=3)
     stream = torch.cuda.ExternalStream(ctx.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -595,6 +602,15 @@ def main():
     if args.form == "serving":
         if rank == 0:
             run_serving(args)
+        return
+    if args.form == "batched":
+        from cadr_gb300 import build, lib
+        build.build()
+        import oracle
+        oracle.build(with_ref=False)
+        ctx = lib.Context(local)
+        print(json.dumps({"form": "batched", **run_batched(ctx, steps=args.steps, warmup=args.warmup,
+                                                           tuning_override=args.batched_tuning)}))
         return
     if args.form == "tier-a":
         from cadr_gb300 import build, lib
