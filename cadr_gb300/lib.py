@@ -106,6 +106,12 @@ _SIGS = {
     "cadr_context_synchronize": ([vp], i32),
     "cadr_context_launch_count": ([vp], u64),
     "cadr_measure_stream_mix": ([vp, u64, u32, C.POINTER(C.c_double)], i32),
+    "cadr_shared_buffer_create": ([vp, sz, C.POINTER(vp)], i32),
+    "cadr_shared_buffer_device_ptr": ([vp], vp),
+    "cadr_shared_buffer_size": ([vp], sz),
+    "cadr_shared_buffer_export_fd": ([vp, C.POINTER(C.c_int)], i32),
+    "cadr_shared_buffer_import_fd": ([vp, C.c_int, sz, C.POINTER(vp)], i32),
+    "cadr_shared_buffer_destroy": ([vp], i32),
     "cadr_context_check_device_error": ([vp, C.POINTER(u32)], i32),
     "cadr_debug_set_fault": ([vp, u32], i32),
     "cadr_context_set_collect_frame_info": ([vp, i32], i32),
@@ -352,6 +358,42 @@ class Context:
     def set_tuning(self, block_threads, items_per_thread, ctas_per_sm):
         t = Tuning(block_threads, items_per_thread, ctas_per_sm, 0)
         check(self.lib.cadr_set_tuning(self.handle, C.byref(t)))
+
+
+class SharedBuffer:
+    """cadr_shared_buffer: device memory a Vulkan device can import by file
+    descriptor.  `ptr` is its device address in this context."""
+
+    def __init__(self, ctx: "Context", nbytes: int = 0, fd: int | None = None, import_bytes: int = 0):
+        """A new buffer of `nbytes`, or with `fd` the import of an exported
+        descriptor of `import_bytes` (the descriptor stays the caller's)."""
+        self.ctx, h = ctx, vp()
+        if fd is not None:
+            check(ctx.lib.cadr_shared_buffer_import_fd(ctx.handle, fd, import_bytes, C.byref(h)))
+        else:
+            check(ctx.lib.cadr_shared_buffer_create(ctx.handle, nbytes, C.byref(h)))
+        self.handle = h.value
+        self.ptr = ctx.lib.cadr_shared_buffer_device_ptr(self.handle)
+        self.nbytes = ctx.lib.cadr_shared_buffer_size(self.handle)
+
+    def __int__(self) -> int:
+        return int(self.ptr)
+
+    def export_fd(self) -> int:
+        fd = C.c_int(-1)
+        check(self.ctx.lib.cadr_shared_buffer_export_fd(self.handle, C.byref(fd)))
+        return fd.value
+
+    def close(self):
+        if self.handle:
+            check(self.ctx.lib.cadr_shared_buffer_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class CullOutputs:

@@ -487,6 +487,33 @@ CADR_API cadr_status cadr_server_poll(cadr_server* srv, cadr_request_result* res
 CADR_API cadr_status cadr_server_release(cadr_server* srv, uint64_t request_id);
 CADR_API cadr_status cadr_server_drain(cadr_server* srv);
 
+/* ------------------------------------------------------------------------ */
+/* Output buffers shared with a Vulkan renderer.  The reference shares
+ * memory between APIs by allocating it exportable and handing an opaque
+ * file descriptor to the importer (examples/OpenGLInteroperability/
+ * main.cpp:1488-1490, 1538-1550, 1616-1619).  A shared buffer is device
+ * memory made for POSIX-FD export and mapped into the context; the pass
+ * writes its commands, counts, indirect records or pointers straight into
+ * it, and a Vulkan device imports the descriptor with
+ * VkImportMemoryFdInfoKHR (VK_EXTERNAL_MEMORY_HANDLE_TYPE_OPAQUE_FD_BIT,
+ * allocationSize = cadr_shared_buffer_size) and draws from it. */
+typedef struct cadr_shared_buffer cadr_shared_buffer;
+/* `bytes` is rounded up to the allocation granularity. */
+CADR_API cadr_status cadr_shared_buffer_create(cadr_context* ctx, size_t bytes, cadr_shared_buffer** out);
+CADR_API void* cadr_shared_buffer_device_ptr(cadr_shared_buffer* buf);
+CADR_API size_t cadr_shared_buffer_size(cadr_shared_buffer* buf);
+/* A new descriptor for every call; the importer owns it (Vulkan takes
+ * ownership on a successful import, otherwise the caller closes it). */
+CADR_API cadr_status cadr_shared_buffer_export_fd(cadr_shared_buffer* buf, int* fd);
+/* Maps an exported descriptor of `bytes` (cadr_shared_buffer_size of the
+ * exporter) into ctx: the same memory at a second address.  The caller
+ * keeps the descriptor and closes it. */
+CADR_API cadr_status cadr_shared_buffer_import_fd(cadr_context* ctx, int fd, size_t bytes,
+                                                  cadr_shared_buffer** out);
+/* Waits for the device, then unmaps and releases (the memory itself lives
+ * on while another mapping or an importer holds it). */
+CADR_API cadr_status cadr_shared_buffer_destroy(cadr_shared_buffer* buf);
+
 #ifdef __cplusplus
 }
 #endif
