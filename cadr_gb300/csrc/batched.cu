@@ -55,19 +55,32 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
     if (t == 0) sm.info[1] = load_relaxed_u32(&s.ctl->epoch);
     uint32_t cur_job = 0xffffffffu;
     const uint32_t* off = nullptr;
+    // Thread 0 takes the next item while the current one's commands are
+    // written, so that the atomic's round trip is off the critical path
+    // (the item is held for one write phase before it starts).
+    uint32_t nxt = 0;
+    bool have_next = false;
     for (;;) {
         if (t == 0) {
-            const uint32_t item = atomicAdd(&s.ctl->tile_counter, 1u);
+            const uint32_t item = have_next ? nxt : atomicAdd(&s.ctl->tile_counter, 1u);
             sm.info[0] = item;
-            uint32_t lo = 0, hi = num_jobs;
-            while (lo < hi) {
+            // Items only grow within a CTA: the job is at or after the
+            // current one.  Gallop forward, then bisect.
+            uint32_t lo = cur_job == 0xffffffffu ? 0u : cur_job, hi = lo + 1, step = 1;
+            while (hi < num_jobs && __ldg(&jobs[hi].first_item) <= item) {
+                lo = hi;
+                step <<= 1;
+                hi = lo + step;
+            }
+            hi = min(hi, num_jobs);
+            while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
                 if (__ldg(&jobs[mid].first_item) <= item)
-                    lo = mid + 1;
+                    lo = mid;
                 else
                     hi = mid;
             }
-            s_job = lo ? lo - 1 : 0;
+            s_job = lo;
         }
         __syncthreads();
         const uint32_t item = sm.info[0];
@@ -115,6 +128,10 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         __syncthreads();
         T::scan(sm, off, job.num_state_sets, b, job.n);
         T::lookback(sm, s.tile_state, item, job.first_item, off, b, limit_ns, fault, error);
+        if (t == 0) {
+            nxt = atomicAdd(&s.ctl->tile_counter, 1u);
+            have_next = true;
+        }
         T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, off, job.num_state_sets,
                  job.lods, job.num_geometries, job.num_lods, job.cmds, job.counts, error);
         __syncthreads();
