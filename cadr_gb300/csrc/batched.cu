@@ -127,13 +127,19 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         }
         __syncthreads();
         T::scan(sm, off, job.num_state_sets, b, job.n);
-        T::lookback(sm, s.tile_state, item, job.first_item, off, b, limit_ns, fault, error);
+        // The aggregate goes out first; the LOD entries are gathered while
+        // warp 0 waits for its predecessor's prefix.
+        if (t == 0) T::publish(sm, s.tile_state, item, job.first_item, off, b, fault);
+        uint4 ent[IPT];
+        T::gather(vis_bits, lod_bits, geo, job.lods, job.num_geometries, job.num_lods, error, ent);
+        if (warp == 0) T::resolve(sm, s.tile_state, item, job.first_item, limit_ns, error);
+        __syncthreads();
         if (t == 0) {
             nxt = atomicAdd(&s.ctl->tile_counter, 1u);
             have_next = true;
         }
-        T::write(sm, vis_bits, lod_bits, geo, b, job.n, item == job.first_item, off, job.num_state_sets,
-                 job.lods, job.num_geometries, job.num_lods, job.cmds, job.counts, error);
+        T::write_ent(sm, vis_bits, ent, b, job.n, item == job.first_item, off, job.num_state_sets, job.cmds,
+                     job.counts, error);
         __syncthreads();
     }
     if (t == 0) finish_pass(s.ctl);

@@ -175,20 +175,6 @@ struct Tile {
         }
     }
 
-    // Warp 0: publish the tile aggregate, look back, publish the inclusive
-    // prefix.  `item` indexes `states`; items in [first, item) precede it in
-    // the same scan.  Ends with __syncthreads(); carry in info[2].
-    __device__ static __forceinline__ void lookback(Smem& sm, uint64_t* __restrict__ states, int64_t item,
-                                                    int64_t first, const uint32_t* __restrict__ offsets, uint32_t b,
-                                                    uint64_t limit_ns, uint32_t fault, uint32_t* error)
-    {
-        if ((threadIdx.x >> 5) == 0) {
-            if ((threadIdx.x & 31) == 0) publish(sm, states, item, first, offsets, b, fault);
-            resolve(sm, states, item, first, limit_ns, error);
-        }
-        __syncthreads();
-    }
-
     // Every thread: the LOD-table entries of its visible items, all issued
     // together so that their L2 round trips overlap.
     __device__ static __forceinline__ void gather(uint32_t vis_bits, uint32_t lod_bits, const uint32_t (&geo)[IPT],
@@ -208,22 +194,9 @@ struct Tile {
         }
     }
 
-    // Every thread: write the commands of its visible items and the counts
-    // of the regions ending in this tile (the scan's first tile also writes
-    // the zero counts of empty regions).
-    __device__ static __forceinline__ void write(const Smem& sm, uint32_t vis_bits, uint32_t lod_bits,
-                                                 const uint32_t (&geo)[IPT], uint32_t b, uint32_t n, bool first_tile,
-                                                 const uint32_t* __restrict__ offsets, uint32_t S,
-                                                 const uint4* __restrict__ lods, uint32_t G, uint32_t L,
-                                                 uint32_t* __restrict__ cmds, uint32_t* __restrict__ counts,
-                                                 uint32_t* error)
-    {
-        uint4 ent[IPT];
-        gather(vis_bits, lod_bits, geo, lods, G, L, error, ent);
-        write_ent(sm, vis_bits, ent, b, n, first_tile, offsets, S, cmds, counts, error);
-    }
-
-    // write() with the LOD entries already gathered.
+    // Every thread: write the commands of its visible items (LOD entries
+    // from gather()) and the counts of the regions ending in this tile (the
+    // scan's first tile also writes the zero counts of empty regions).
     __device__ static __forceinline__ void write_ent(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[IPT],
                                                      uint32_t b, uint32_t n, bool first_tile,
                                                      const uint32_t* __restrict__ offsets, uint32_t S,
