@@ -80,6 +80,13 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint3
                 load_mat(a.local + (size_t)i * 4, l0, l1, l2, l3);
                 const float4 sp = ld_nc_f4(a.sphere + i);
                 if (a.parent) {
+                    // Launched as a programmatic dependent of the last
+                    // level kernel, the stream kernel reads that level's
+                    // world matrices only once it has completed; the loads
+                    // above (parent indices, the first row's records) and
+                    // the tile's region start overlap its tail.  Without
+                    // the launch attribute this is a no-op.
+                    if (j == 0) grid_dependency_wait();
                     uint32_t p = par[j];
                     if (p >= a.num_parents) {
                         atomicOr(a.error, CADR_DEVERR_BAD_INDEX);
@@ -334,6 +341,10 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
     __shared__ uint32_t s_plo, s_cnt;
     __shared__ int s_ok;
 
+    // A programmatic dependent (the plain pass's stream kernel after the
+    // last level) may launch now: it reads this level's world matrices
+    // only after griddepcontrol.wait.
+    grid_dependents_launch();
     const uint32_t b = blockIdx.x * (uint32_t)kPropThreads;
     const uint32_t i = b + threadIdx.x;
     bool use_stage = false;
@@ -410,14 +421,29 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream)
+cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
+                             bool after_level_kernel)
 {
     if (a.n == 0) return cudaSuccess;
     const uint32_t tiles = (a.n + kLeafTile - 1) / kLeafTile;
     LeafArgs b = a;
     b.planes = s.planes;
     b.tile_words = reinterpret_cast<uint32_t*>(s.tile_state);
-    leaf_stream_kernel<<<tiles, kLeafThreads, 0, stream>>>(b);
+    if (after_level_kernel) {
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at.val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cf = {};
+        cf.gridDim = dim3(tiles);
+        cf.blockDim = dim3(kLeafThreads);
+        cf.stream = stream;
+        cf.attrs = &at;
+        cf.numAttrs = 1;
+        const cudaError_t el = cudaLaunchKernelEx(&cf, leaf_stream_kernel, b);
+        if (el != cudaSuccess) return el;
+    } else {
+        leaf_stream_kernel<<<tiles, kLeafThreads, 0, stream>>>(b);
+    }
     if (after_stream) {
         const cudaError_t er = cudaEventRecord(after_stream, stream);
         if (er != cudaSuccess) return er;

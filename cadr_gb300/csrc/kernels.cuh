@@ -81,8 +81,12 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 // select LOD, compact per StateSet.  Three launches on `stream`; needs
 // s.tile_state for ceil(n / kLeafTile) words and s.planes for
 // leaf_plane_words(n).  `after_stream`, when not null, is recorded on
-// `stream` between the stream kernel and the tile scan.
-cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream);
+// `stream` between the stream kernel and the tile scan.  With
+// `after_level_kernel` (the launch just before on `stream` is the last
+// level's propagate_kernel) the stream kernel is launched as its
+// programmatic dependent.
+cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
+                             bool after_level_kernel = false);
 constexpr uint32_t kLeafCullLaunches = 3;
 // Words of one bit-plane (one per 32 drawables), padded to 16 bytes.
 __host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 31) / 32 + 3) & ~uint64_t(3); }

@@ -364,7 +364,9 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
     a.counts = counts;
     a.marginal = marginal;
     a.view = to_view_const(*view);
-    e = launch_leaf_cull(a, ctx->scratch, s, fev ? fev[2] : nullptr);
+    // The stream kernel overlaps the last level kernel's tail when that
+    // kernel is the launch just before it (no frame-timing event between).
+    e = launch_leaf_cull(a, ctx->scratch, s, fev ? fev[2] : nullptr, !fev && sc->desc.num_levels >= 2);
     if (e != cudaSuccess) return cuda_fail(e, "cull: launch");
     ctx->launches += kLeafCullLaunches;
     if (fev) {
