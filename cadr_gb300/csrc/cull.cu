@@ -341,17 +341,31 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
     __shared__ uint32_t s_plo, s_cnt;
     __shared__ int s_ok;
 
-    // A programmatic dependent (the plain pass's stream kernel after the
-    // last level) may launch now: it reads this level's world matrices
-    // only after griddepcontrol.wait.
+    // A programmatic dependent (the next level, or the plain pass's stream
+    // kernel after the last level) may launch now: it reads this level's
+    // world matrices only after griddepcontrol.wait.
     grid_dependents_launch();
     const uint32_t b = blockIdx.x * (uint32_t)kPropThreads;
     const uint32_t i = b + threadIdx.x;
+    // This node's inputs do not depend on the previous level: they are in
+    // flight while it finishes (when this kernel is its programmatic
+    // dependent; otherwise the wait below is a no-op).
+    uint32_t p = 0;
+    float4 l0 = {}, l1 = {}, l2 = {}, l3 = {};
+    if (i < n) {
+        p = __ldg(parent + i);
+        load_mat(local + (size_t)i * 4, l0, l1, l2, l3);
+    }
+    uint32_t plo = 0, phi = 0;
+    if (staged && threadIdx.x == 0) {
+        const uint32_t last = min(b + (uint32_t)kPropThreads, n) - 1;
+        plo = __ldg(parent + b);
+        phi = __ldg(parent + last);
+    }
+    grid_dependency_wait();
     bool use_stage = false;
     if (staged) {
         if (threadIdx.x == 0) {
-            const uint32_t last = min(b + (uint32_t)kPropThreads, n) - 1;
-            const uint32_t plo = __ldg(parent + b), phi = __ldg(parent + last);
             const uint32_t cnt = phi - plo + 1;
             const int ok = (phi >= plo) && (phi < np) && (cnt <= kMaxStaged);
             s_plo = plo;
@@ -372,7 +386,6 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
         }
     }
     if (i >= n) return;
-    uint32_t p = __ldg(parent + i);
     if (p >= np) {
         atomicOr(error, CADR_DEVERR_BAD_INDEX);
         p = 0;
@@ -391,8 +404,6 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
         p2 = __ldg(pp + 2);
         p3 = __ldg(pp + 3);
     }
-    float4 l0, l1, l2, l3;
-    load_mat(local + (size_t)i * 4, l0, l1, l2, l3);
     // Default-cached stores: the next level (or the leaf pass) gathers
     // these matrices as parents while they are still in L2.
     float4* wp = world + (size_t)i * 4;
@@ -404,13 +415,27 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
 
 cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, const float4* local,
                              const uint32_t* parent, uint32_t n, float4* world, int staged,
-                             uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream)
+                             uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream,
+                             bool after_level_kernel)
 {
     if (n == 0) return cudaSuccess;
     const uint32_t grid = (n + kPropThreads - 1) / kPropThreads;
-    propagate_kernel<<<grid, kPropThreads, 0, stream>>>(parent_world, num_parents, local, parent, n,
-                                                        world, staged, error, spin_limit_ns);
-    return cudaGetLastError();
+    if (!after_level_kernel) {
+        propagate_kernel<<<grid, kPropThreads, 0, stream>>>(parent_world, num_parents, local, parent, n,
+                                                            world, staged, error, spin_limit_ns);
+        return cudaGetLastError();
+    }
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cf = {};
+    cf.gridDim = dim3(grid);
+    cf.blockDim = dim3(kPropThreads);
+    cf.stream = stream;
+    cf.attrs = &at;
+    cf.numAttrs = 1;
+    return cudaLaunchKernelEx(&cf, propagate_kernel, parent_world, num_parents, local, parent, n, world, staged,
+                              error, spin_limit_ns);
 }
 
 cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)

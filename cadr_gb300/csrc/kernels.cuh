@@ -70,9 +70,13 @@ constexpr int kPropThreads = 256;
 
 // Internal level: world[i] = parent_world[parent[i]] * local[i].
 // staged != 0 asserts non-decreasing parents (bulk copy of the parent run).
+// With `after_level_kernel` (the launch just before on `stream` is the
+// previous level's propagate_kernel) it is launched as that kernel's
+// programmatic dependent.
 cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, const float4* local,
                              const uint32_t* parent, uint32_t n, float4* world, int staged,
-                             uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream);
+                             uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream,
+                             bool after_level_kernel = false);
 
 // Leaf level propagation (+ optional world spheres) without culling.
 cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);

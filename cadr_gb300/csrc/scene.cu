@@ -117,7 +117,7 @@ cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
             reinterpret_cast<const float4*>(sc->buf.level_world[l - 1]), (uint32_t)sc->desc.level_size[l - 1],
             reinterpret_cast<const float4*>(sc->buf.level_local[l]), sc->buf.level_parent[l],
             (uint32_t)sc->desc.level_size[l], reinterpret_cast<float4*>(sc->buf.level_world[l]), 1,
-            ctx->d_error, ctx->spin_limit_ns, stream);
+            ctx->d_error, ctx->spin_limit_ns, stream, l >= 2);
         if (e != cudaSuccess) return cuda_fail(e, "propagate: launch");
         if (sc->desc.level_size[l]) ctx->launches++;
     }
