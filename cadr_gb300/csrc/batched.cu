@@ -267,6 +267,7 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
                                        const cadr_tuning* tuning, int use_graph, cadr_stream stream)
 {
     if (!ctx || (!views && num_views)) return fail(CADR_ERR_INVALID_ARG, "cull_batched: null argument");
+    DeviceGuard dg(ctx->device);
     if (num_views == 0) return CADR_OK;
     const cadr_tuning tu = tuning ? *tuning : ctx->tuning;
     if (!tuning_valid(tu)) return fail(CADR_ERR_INVALID_ARG, "cull_batched: unsupported tuning");
@@ -370,6 +371,7 @@ CADR_API cadr_status cadr_autotune_batched(cadr_context* ctx, const cadr_batch_v
                                            uint32_t reps, cadr_tuning* best, float* best_ms)
 {
     if (!ctx || !views || num_views == 0 || !best) return fail(CADR_ERR_INVALID_ARG, "autotune: bad argument");
+    DeviceGuard dg(ctx->device);
     if (reps == 0) reps = 5;
     const uint32_t threads[] = {128, 256, 512};
     const uint32_t ipts[] = {4, 8, 16};

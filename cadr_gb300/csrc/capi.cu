@@ -177,7 +177,8 @@ CADR_API cadr_status cadr_context_create(int device, cadr_context** out)
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess) return cuda_fail(e, "context_create: no CUDA device");
     if (device < 0 || device >= count) return fail(CADR_ERR_INVALID_ARG, "context_create: bad device %d", device);
-    e = cudaSetDevice(device);
+    DeviceGuard dg(device);
+    e = dg.error();
     if (e != cudaSuccess) return cuda_fail(e, "context_create: set device");
     auto* ctx = new cadr_context();
     ctx->device = device;
@@ -209,7 +210,7 @@ CADR_API cadr_status cadr_context_create(int device, cadr_context** out)
 CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
 {
     if (!ctx) return CADR_OK;
-    cudaSetDevice(ctx->device);
+    DeviceGuard dg(ctx->device);
     cudaDeviceSynchronize();
     destroy_batched_state(ctx);
     scratch_release(ctx->scratch);
@@ -241,6 +242,7 @@ CADR_API cadr_status cadr_context_set_spin_limit_ns(cadr_context* ctx, uint64_t 
 CADR_API cadr_status cadr_context_synchronize(cadr_context* ctx)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "synchronize: null context");
+    DeviceGuard dg(ctx->device);
     cudaError_t e = cudaStreamSynchronize(ctx->upload_stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "synchronize");
@@ -252,6 +254,7 @@ CADR_API uint64_t cadr_context_launch_count(cadr_context* ctx) { return ctx ? ct
 CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t* error_bits)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "check_device_error: null context");
+    DeviceGuard dg(ctx->device);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "check_device_error: synchronize");
     const uint32_t bits = *reinterpret_cast<volatile uint32_t*>(ctx->h_error);
@@ -268,6 +271,7 @@ CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t
 CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int on)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "set_collect_frame_info: null context");
+    DeviceGuard dg(ctx->device);
     if (on && !ctx->frame_ev[0][0]) {
         for (int f = 0; f < cadr_context::kFrames; f++)
             for (int k = 0; k < 4; k++) {
@@ -284,6 +288,7 @@ CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_
                                                   uint32_t* num_frames)
 {
     if (!ctx || !num_frames || (!out && max_frames)) return fail(CADR_ERR_INVALID_ARG, "get_frame_infos: bad argument");
+    DeviceGuard dg(ctx->device);
     uint32_t k = 0;
     while (k < max_frames && ctx->frame_tail < ctx->frame_head) {
         cudaEvent_t* ev = ctx->frame_ev[ctx->frame_tail % cadr_context::kFrames];
@@ -311,9 +316,9 @@ CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault)
 CADR_API cadr_status cadr_device_alloc(cadr_context* ctx, size_t bytes, void** out)
 {
     if (!ctx || !out) return fail(CADR_ERR_INVALID_ARG, "device_alloc: null argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
     if (bytes == 0) return CADR_OK;
-    cudaSetDevice(ctx->device);
     cudaError_t e = cudaMalloc(out, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "device_alloc");
     return CADR_OK;
@@ -322,6 +327,7 @@ CADR_API cadr_status cadr_device_alloc(cadr_context* ctx, size_t bytes, void** o
 CADR_API cadr_status cadr_device_free(cadr_context* ctx, void* ptr)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "device_free: null context");
+    DeviceGuard dg(ctx->device);
     if (!ptr) return CADR_OK;
     cudaError_t e = cudaFree(ptr);
     if (e != cudaSuccess) return cuda_fail(e, "device_free");
@@ -348,6 +354,7 @@ CADR_API cadr_status cadr_upload(cadr_context* ctx, void* dst_device, const void
                                  cadr_stream stream)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "upload: null context");
+    DeviceGuard dg(ctx->device);
     return upload_bytes(ctx, dst_device, src_host, bytes, pick_stream(ctx, stream));
 }
 
@@ -355,6 +362,7 @@ CADR_API cadr_status cadr_download(cadr_context* ctx, void* dst_host, const void
                                    cadr_stream stream)
 {
     if (!ctx || (!dst_host && bytes) || (!src_device && bytes)) return fail(CADR_ERR_INVALID_ARG, "download: bad argument");
+    DeviceGuard dg(ctx->device);
     if (bytes == 0) return CADR_OK;
     cudaError_t e = cudaMemcpyAsync(dst_host, src_device, bytes, cudaMemcpyDeviceToHost, pick_stream(ctx, stream));
     if (e != cudaSuccess) return cuda_fail(e, "download");
@@ -377,6 +385,7 @@ CADR_API cadr_status cadr_process_drawables(cadr_context* ctx, uint32_t handle_l
                                             cadr_stream stream)
 {
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "process_drawables: null context");
+    DeviceGuard dg(ctx->device);
     if (handle_level < 1 || handle_level > 3)
         return fail(CADR_ERR_INVALID_ARG, "process_drawables: handle level %u not in 1..3", handle_level);
     if (num_drawables == 0) return CADR_OK;

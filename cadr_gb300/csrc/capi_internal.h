@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "device_guard.h"
 #include "kernels.cuh"
 
 namespace cadr {

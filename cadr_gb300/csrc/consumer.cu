@@ -144,6 +144,7 @@ CADR_API cadr_status cadr_check_draws(cadr_context* ctx, const cadr_draw_indirec
 {
     if (!ctx || !view || (num_draws && (!indirect || !pointers || !out)) || (num_regions && !regions))
         return fail(CADR_ERR_INVALID_ARG, "check_draws: null argument");
+    DeviceGuard dg(ctx->device);
     if (num_regions > CADR_MAX_MEMORY_REGIONS)
         return fail(CADR_ERR_INVALID_ARG, "check_draws: %u regions exceed %u", num_regions, CADR_MAX_MEMORY_REGIONS);
     if ((reinterpret_cast<uintptr_t>(indirect) | reinterpret_cast<uintptr_t>(out)) % 16 ||

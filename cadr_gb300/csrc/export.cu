@@ -152,8 +152,8 @@ extern "C" {
 CADR_API cadr_status cadr_shared_buffer_create(cadr_context* ctx, size_t bytes, cadr_shared_buffer** out)
 {
     if (!ctx || !out || bytes == 0) return fail(CADR_ERR_INVALID_ARG, "shared_buffer_create: bad argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
-    cudaSetDevice(ctx->device);
     size_t gran = 0;
     cadr_status st = check_support(ctx, &gran);
     if (st != CADR_OK) return st;
@@ -180,8 +180,8 @@ CADR_API cadr_status cadr_shared_buffer_create(cadr_context* ctx, size_t bytes, 
 CADR_API cadr_status cadr_shared_buffer_import_fd(cadr_context* ctx, int fd, size_t bytes, cadr_shared_buffer** out)
 {
     if (!ctx || !out || fd < 0 || bytes == 0) return fail(CADR_ERR_INVALID_ARG, "shared_buffer_import_fd: bad argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
-    cudaSetDevice(ctx->device);
     size_t gran = 0;
     cadr_status st = check_support(ctx, &gran);
     if (st != CADR_OK) return st;
@@ -227,7 +227,7 @@ CADR_API size_t cadr_shared_buffer_size(cadr_shared_buffer* b) { return b ? b->b
 CADR_API cadr_status cadr_shared_buffer_destroy(cadr_shared_buffer* b)
 {
     if (!b) return CADR_OK;
-    cudaSetDevice(b->ctx->device);
+    DeviceGuard dg(b->ctx->device);
     // Work on the buffer may still be queued: it finishes before the
     // mapping goes.
     const cudaError_t e = cudaDeviceSynchronize();

@@ -241,8 +241,9 @@ extern "C" {
 CADR_API cadr_status cadr_pack_create(cadr_context* ctx, uint32_t capacity, cadr_pack** out)
 {
     if (!ctx || !out) return fail(CADR_ERR_INVALID_ARG, "pack_create: null argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
-    cudaError_t e = cudaSetDevice(ctx->device);
+    cudaError_t e = dg.error();
     if (e != cudaSuccess) return cuda_fail(e, "pack_create: set device");
     auto* pk = new cadr_pack();
     pk->ctx = ctx;
@@ -267,7 +268,7 @@ CADR_API cadr_status cadr_pack_create(cadr_context* ctx, uint32_t capacity, cadr
 CADR_API cadr_status cadr_pack_destroy(cadr_pack* pack)
 {
     if (!pack) return CADR_OK;
-    cudaSetDevice(pack->ctx->device);
+    DeviceGuard dg(pack->ctx->device);
     cudaDeviceSynchronize();
     release(pack);
     delete pack;
@@ -280,6 +281,7 @@ CADR_API cadr_status cadr_pack_set_layout(cadr_pack* pk, uint32_t num_slots, uin
 {
     if (!pk || !dfs_order || (num_slots && (!state_set_of_slot || !list_index_of_slot)))
         return fail(CADR_ERR_INVALID_ARG, "pack_set_layout: null argument");
+    DeviceGuard dg(pk->ctx->device);
     if (num_slots > pk->capacity)
         return fail(CADR_ERR_INVALID_ARG, "pack_set_layout: %u slots exceed the capacity %u", num_slots,
                     pk->capacity);
@@ -332,6 +334,7 @@ CADR_API cadr_status cadr_pack_upload(cadr_pack* pk, const cadr_drawable_gpu_dat
                                       uint32_t count, cadr_stream stream)
 {
     if (!pk || (count && !records)) return fail(CADR_ERR_INVALID_ARG, "pack_upload: null argument");
+    DeviceGuard dg(pk->ctx->device);
     if ((uint64_t)first + count > pk->capacity)
         return fail(CADR_ERR_INVALID_ARG, "pack_upload: slots [%u, %llu) exceed the capacity %u", first,
                     (unsigned long long)first + count, pk->capacity);
@@ -342,6 +345,7 @@ CADR_API cadr_status cadr_pack_upload(cadr_pack* pk, const cadr_drawable_gpu_dat
 CADR_API cadr_status cadr_pack_repack(cadr_pack* pk, cadr_stream stream)
 {
     if (!pk) return fail(CADR_ERR_INVALID_ARG, "pack_repack: null pack");
+    DeviceGuard dg(pk->ctx->device);
     if (pk->num_slots == 0) return CADR_OK;
     cudaStream_t s = pick_stream(pk->ctx, stream);
     pack_gather_kernel<<<blocks(3ull * pk->num_slots), kPackThreads, 0, s>>>(pk->pool, pk->slot_of_pos, pk->num_slots,
@@ -356,6 +360,7 @@ CADR_API cadr_status cadr_pack_patch(cadr_pack* pk, const uint32_t* slots, const
                                      uint32_t count, cadr_stream stream)
 {
     if (!pk || (count && (!slots || !records))) return fail(CADR_ERR_INVALID_ARG, "pack_patch: null argument");
+    DeviceGuard dg(pk->ctx->device);
     if (count == 0) return CADR_OK;
     cadr_context* ctx = pk->ctx;
     cudaStream_t s = pick_stream(ctx, stream);
@@ -393,6 +398,7 @@ CADR_API cadr_status cadr_pack_process_drawables(cadr_pack* pk, uint32_t handle_
 {
     if (!pk || (num_draw_records && (!handle_table || !indirect || !pointers)))
         return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: null argument");
+    DeviceGuard dg(pk->ctx->device);
     if (handle_level < 1 || handle_level > 3)
         return fail(CADR_ERR_INVALID_ARG, "pack_process_drawables: handle level %u", handle_level);
     if (num_draw_records > pk->num_slots)

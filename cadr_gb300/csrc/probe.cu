@@ -62,9 +62,9 @@ CADR_API cadr_status cadr_measure_stream_mix(cadr_context* ctx, uint64_t num_dra
 {
     if (!ctx || !gbytes_per_s || num_drawables == 0 || num_drawables > 0xffffffffull || reps == 0)
         return fail(CADR_ERR_INVALID_ARG, "measure_stream_mix: bad argument");
+    DeviceGuard dg(ctx->device);
     const uint64_t n = num_drawables;
     const size_t bytes = (size_t)n * (64 + 16 + 4 + 64) + 3 * 256 + 4;
-    cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     uint8_t* base = nullptr;
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&base), bytes, s);

@@ -154,6 +154,7 @@ extern "C" {
 CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc* desc, cadr_scene** out)
 {
     if (!ctx || !desc || !out) return fail(CADR_ERR_INVALID_ARG, "scene_create: null argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
     const cadr_scene_desc& d = *desc;
     if (d.num_levels > CADR_MAX_LEVELS) return fail(CADR_ERR_INVALID_ARG, "scene_create: too many levels");
@@ -186,7 +187,6 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     auto* sc = new cadr_scene();
     sc->ctx = ctx;
     sc->desc = d;
-    cudaSetDevice(ctx->device);
     cudaError_t e = cudaMalloc(&sc->arena, off ? off : 256);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sc->uploaded, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sc->read_done, cudaEventDisableTiming);
@@ -225,7 +225,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
 CADR_API cadr_status cadr_scene_destroy(cadr_scene* sc)
 {
     if (!sc) return CADR_OK;
-    cudaSetDevice(sc->ctx->device);
+    DeviceGuard dg(sc->ctx->device);
     cudaDeviceSynchronize();
     if (sc->arena) cudaFree(sc->arena);
     if (sc->uploaded) cudaEventDestroy(sc->uploaded);
@@ -246,6 +246,7 @@ CADR_API cadr_status cadr_scene_upload_level(cadr_scene* sc, uint32_t level, con
                                              const uint32_t* parent, uint64_t first, uint64_t count)
 {
     if (!sc || level >= sc->desc.num_levels) return fail(CADR_ERR_INVALID_ARG, "scene_upload_level: bad level");
+    DeviceGuard dg(sc->ctx->device);
     const uint64_t n = sc->desc.level_size[level];
     if (first > n || count > n - first) return fail(CADR_ERR_INVALID_ARG, "scene_upload_level: rows out of range");
     if (level == 0 && parent) return fail(CADR_ERR_INVALID_ARG, "scene_upload_level: level 0 has no parents");
@@ -264,6 +265,7 @@ CADR_API cadr_status cadr_scene_upload_drawables(cadr_scene* sc, const float* lo
                                                  uint64_t count)
 {
     if (!sc) return fail(CADR_ERR_INVALID_ARG, "scene_upload_drawables: null scene");
+    DeviceGuard dg(sc->ctx->device);
     const uint64_t n = sc->desc.num_drawables;
     if (first > n || count > n - first) return fail(CADR_ERR_INVALID_ARG, "scene_upload_drawables: rows out of range");
     if (parent && !sc->desc.num_levels) return fail(CADR_ERR_INVALID_ARG, "scene_upload_drawables: scene has no hierarchy");
@@ -282,6 +284,7 @@ CADR_API cadr_status cadr_scene_upload_drawables(cadr_scene* sc, const float* lo
 CADR_API cadr_status cadr_scene_upload_state_sets(cadr_scene* sc, const uint32_t* offsets)
 {
     if (!sc || !offsets) return fail(CADR_ERR_INVALID_ARG, "scene_upload_state_sets: null argument");
+    DeviceGuard dg(sc->ctx->device);
     const uint32_t S = sc->desc.num_state_sets;
     if (offsets[0] != 0 || offsets[S] != sc->desc.num_drawables)
         return fail(CADR_ERR_INVALID_ARG, "scene_upload_state_sets: offsets must start at 0 and end at N");
@@ -297,6 +300,7 @@ CADR_API cadr_status cadr_scene_upload_state_sets(cadr_scene* sc, const uint32_t
 CADR_API cadr_status cadr_scene_upload_lods(cadr_scene* sc, const cadr_lod* lods)
 {
     if (!sc || !lods) return fail(CADR_ERR_INVALID_ARG, "scene_upload_lods: null argument");
+    DeviceGuard dg(sc->ctx->device);
     cadr_status st = before_upload(sc);
     if (st != CADR_OK) return st;
     st = upload_bytes(sc->ctx, sc->buf.lods, lods,
@@ -308,12 +312,14 @@ CADR_API cadr_status cadr_scene_upload_lods(cadr_scene* sc, const cadr_lod* lods
 CADR_API cadr_status cadr_scene_commit(cadr_scene* sc)
 {
     if (!sc) return fail(CADR_ERR_INVALID_ARG, "scene_commit: null scene");
+    DeviceGuard dg(sc->ctx->device);
     return commit(sc);
 }
 
 CADR_API cadr_status cadr_scene_propagate(cadr_scene* sc, int write_world_spheres, cadr_stream stream)
 {
     if (!sc) return fail(CADR_ERR_INVALID_ARG, "scene_propagate: null scene");
+    DeviceGuard dg(sc->ctx->device);
     cudaStream_t s = pick_stream(sc->ctx, stream);
     cadr_status st = scene_prepare(sc, s);
     if (st != CADR_OK) return st;
@@ -332,6 +338,7 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
 {
     if (!sc || !view || !counts || (!cmds && sc->desc.num_drawables))
         return fail(CADR_ERR_INVALID_ARG, "cull: null argument");
+    DeviceGuard dg(sc->ctx->device);
     cadr_context* ctx = sc->ctx;
     cudaStream_t s = pick_stream(ctx, stream);
     cadr_status st = scene_prepare(sc, s);

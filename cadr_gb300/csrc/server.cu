@@ -220,6 +220,8 @@ static cadr_status launch_slot(cadr_server* srv, Slot* slot, std::vector<Request
 
 static void worker_main(cadr_server* srv)
 {
+    // The scheduler thread belongs to the server: its current device is
+    // the context's for its whole life (no caller's device to keep).
     cudaSetDevice(srv->ctx->device);
     std::unique_lock<std::mutex> lk(srv->mu);
     for (;;) {
@@ -292,13 +294,13 @@ extern "C" {
 CADR_API cadr_status cadr_server_create(cadr_context* ctx, const cadr_server_config* cfg, cadr_server** out)
 {
     if (!ctx || !cfg || !out) return fail(CADR_ERR_INVALID_ARG, "server_create: null argument");
+    DeviceGuard dg(ctx->device);
     *out = nullptr;
     if (cfg->max_inflight_batches == 0 || cfg->max_inflight_batches > 16 || cfg->max_batch_views == 0)
         return fail(CADR_ERR_INVALID_ARG, "server_create: 1..16 batches in flight and >= 1 view per batch");
     auto* srv = new cadr_server();
     srv->ctx = ctx;
     srv->cfg = *cfg;
-    cudaSetDevice(ctx->device);
     size_t budget = cfg->memory_budget_bytes;
     if (budget == 0) {
         size_t fr = 0, tot = 0;
@@ -338,6 +340,7 @@ CADR_API cadr_status cadr_server_create(cadr_context* ctx, const cadr_server_con
 CADR_API cadr_status cadr_server_destroy(cadr_server* srv)
 {
     if (!srv) return CADR_OK;
+    DeviceGuard dg(srv->ctx->device);
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         srv->stop = true;
@@ -350,7 +353,6 @@ CADR_API cadr_status cadr_server_destroy(cadr_server* srv)
     }
     srv->cv.notify_all();
     if (srv->worker.joinable()) srv->worker.join();
-    cudaSetDevice(srv->ctx->device);
     for (Slot* s : srv->slots) {
         if (s->stream) cudaStreamSynchronize(s->stream);
     }

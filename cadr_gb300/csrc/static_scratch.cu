@@ -39,17 +39,18 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void* g_scratch_address[kMaxDevices] = {};
 
-// Set-up on the first call per device, with that device current.
+// Set-up on the first call per device.  The caller (the entry point, under
+// its DeviceGuard) has made `device` current, so the symbol's address is
+// that device's copy of the array; the guard gives the calling thread its
+// own device back afterwards, on the error paths too.
 cadr_status static_scratch_address(int device, void** out)
 {
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (device < 0 || device >= kMaxDevices)
         return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: device %d out of range", device);
     if (!g_scratch_address[device]) {
-        cudaError_t e = cudaSetDevice(device);
-        if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: set device");
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_static_scratch);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: scratch address");
         g_scratch_address[device] = p;
     }
@@ -67,6 +68,7 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
 {
     if (!sc || !view || !counts || (!cmds && sc->desc.num_drawables))
         return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: null argument");
+    DeviceGuard dg(sc->ctx->device);
     if (!sc->committed)
         return fail(CADR_ERR_INVALID_ARG, "cull_static_scratch: commit the scene (cadr_scene_commit) first");
     if (sc->desc.num_drawables > kStaticMaxDrawables)
@@ -92,6 +94,14 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
     scratch.capacity = kStaticMaxTiles;
     scratch.planes = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kTileBytes);
     scratch.plane_words = leaf_plane_words(kStaticMaxDrawables);
+    // Ordered after the context's previous plain pass (cadr_cull or this
+    // entry point, on any stream), as cadr_cull is: passes over one scene
+    // rewrite its world matrices.  Waiting on and recording an event
+    // allocates nothing.
+    if (ctx->pass_recorded) {
+        e = cudaStreamWaitEvent(s, ctx->pass_done, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: order after previous pass");
+    }
     st = propagate_levels(sc, s);
     if (st != CADR_OK) return st;
     LeafArgs a = leaf_args(sc);
@@ -99,9 +109,14 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* sc, const cadr_view* v
     a.counts = counts;
     a.marginal = marginal;
     a.view = to_view_const(*view);
-    e = launch_leaf_cull(a, scratch, s, nullptr);
+    // The same launch sequence as cadr_cull: the stream kernel is a
+    // programmatic dependent of the last level kernel when there is one.
+    e = launch_leaf_cull(a, scratch, s, nullptr, sc->desc.num_levels >= 2);
     if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: launch");
     ctx->launches += kLeafCullLaunches;
+    e = cudaEventRecord(ctx->pass_done, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cull_static_scratch: record");
+    ctx->pass_recorded = true;
     return scene_mark_read(sc, s);
 }
 

@@ -386,8 +386,11 @@ CADR_API cadr_status cadr_cull(cadr_scene* scene, const cadr_view* view,
  * CADR_ERR_INVALID_ARG, as are scenes not committed yet.  The first call on
  * a device looks up the array's device address (set-up): make that first
  * call before any stream capture.  Every call shares the one array, so
- * calls whose work overlaps on the GPU race: keep them on one stream or
- * otherwise ordered. */
+ * calls whose work overlaps on the GPU race.  Each call is ordered after the
+ * context's previous plain pass (cadr_cull or this entry point, on any
+ * stream), as cadr_cull calls are; calls through different contexts on one
+ * device, and cadr_scene_propagate on the same scene from another stream,
+ * must be ordered by the caller. */
 CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* scene, const cadr_view* view,
                                               cadr_draw_indexed_cmd* cmds, uint32_t* counts,
                                               uint32_t* marginal, cadr_stream stream);

@@ -13,7 +13,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcadr_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libcadr_ref.so")
-REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root() -> str:
+    """Location of the CADR reference sources: $CADR_REFERENCE_ROOT, else
+    the default of the build recipe (oracle/Makefile); "" when neither
+    holds the sources."""
+    root = os.environ.get("CADR_REFERENCE_ROOT", "")
+    if not root:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                           capture_output=True, text=True)
+        root = r.stdout.strip() if r.returncode == 0 else ""
+    return root if root and os.path.isdir(os.path.join(root, "src", "CadR")) else ""
+
 
 _lib = None
 _ref = None
@@ -23,8 +35,8 @@ def build(with_ref: bool = True) -> None:
     """Compiles the oracle (and, when the CADR sources are present, the
     reference shim) with oracle/Makefile."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if with_ref and os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "CadR")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_ROOT}"], check=True)
+    if with_ref:
+        subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "ref-if-present"], check=True)
 
 
 def _p(a):

@@ -8,12 +8,14 @@ every call reuses the same static scratch array.  This file is collected
 last so that a run stopping at the first failure has run every other test.
 """
 import ctypes
+import dataclasses
 
 import numpy as np
 import pytest
 
 from cadr_gb300 import lib, scenes
 from helpers import assert_same
+from oracle import bind
 
 pytestmark = pytest.mark.gpu
 
@@ -35,6 +37,35 @@ def test_static_scratch_matches_cull_twice(ctx):
     ctx.check_device_error()
     ref = ref_out.fetch()
     for _ in range(2):  # two calls in a row share the static scratch
+        out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+        _static_cull(ctx, ds, sc.views[0], out)
+        ctx.sync()
+        ctx.check_device_error()
+        assert_same(out.fetch(), ref, sc.state_set_offsets)
+
+
+def test_static_scratch_second_scan_chunk(ctx):
+    """Past 16,777,216 drawables the tile scan takes its tiles in a second
+    chunk (8,192 tiles of 2,048 drawables per chunk) and carries the running
+    region count across.  Region boundaries are placed inside that second
+    chunk (in its first and third tile, with an empty region between) so
+    that the carry, the restart at a region start and the upper part of the
+    static tile and plane areas are all used; both entry points must equal
+    the oracle, twice in a row."""
+    n = (1 << 24) + 3 * 2048 + 777
+    chunk = 8192 * 2048
+    base = scenes.config2(n=n, num_state_sets=5)
+    offsets = np.array([0, 6_000_000, chunk + 700, chunk + 2 * 2048 + 5, chunk + 2 * 2048 + 5, n], np.uint32)
+    sc = dataclasses.replace(base, state_set_offsets=offsets)
+    ref = bind.cull(sc, sc.views[0], threads=bind.max_threads())
+    assert ref["counts"][2] > 0 and ref["counts"][3] == 0 and ref["counts"][4] > 0
+    ds = lib.DeviceScene(ctx, sc)
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    ds.cull(sc.views[0], out)
+    ctx.sync()
+    ctx.check_device_error()
+    assert_same(out.fetch(), ref, sc.state_set_offsets)
+    for _ in range(2):
         out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
         _static_cull(ctx, ds, sc.views[0], out)
         ctx.sync()
