@@ -239,6 +239,10 @@ __device__ __forceinline__ float4 transform_sphere(const float4 m0, const float4
 }
 
 // Plane test, marginal band and LOD (same spec as the oracle's classify).
+// A sphere is marginal when its surface lies within kMarginalBand of a
+// plane: |dist + r| <= 1e-5, in world units.
+constexpr float kMarginalBand = 1e-5f;
+
 __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, uint32_t num_lods,
                                          bool& visible, bool& marginal, uint32_t& lod)
 {
@@ -249,9 +253,7 @@ __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, ui
         const float4 pl = v.plane[p];
         const float dist = fadd(fadd(fadd(fmul(pl.x, ws.x), fmul(pl.y, ws.y)), fmul(pl.z, ws.z)), pl.w);
         vis = vis && (dist >= nr);
-        const float t = fadd(dist, ws.w);
-        const float tol = fmul(1e-5f, fmaxf(1.0f, fadd(fabsf(pl.w), ws.w)));
-        mar = mar || (fabsf(t) <= tol);
+        mar = mar || (fabsf(fadd(dist, ws.w)) <= kMarginalBand);
     }
     float zc = 1.0f;
     if (v.perspective) {

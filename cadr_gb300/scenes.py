@@ -366,3 +366,42 @@ def small_scene(seed: int, n: int, num_levels: int = 2, num_state_sets: int = 5,
                          (48.0, 12.0, 3.0)[:num_lods - 1])
     sc.views = [cam.to_view()]
     return sc
+
+
+def band_scene(seed: int, n: int) -> Scene:
+    """Parity-test scene for the marginal band: n spheres placed against the
+    six planes of C1's camera, each at a signed surface distance
+    t = dist + r drawn from U[-4e-5, 4e-5] from one plane (computed in
+    double, stored as float translations of identity leaf matrices, no
+    hierarchy), so that a good share of them lies inside the 1e-5 band and
+    the rest just outside it.  Points are taken at depths up to 20 units,
+    where a float coordinate still resolves the band."""
+    view = config1().views[0]
+    planes = view["planes"].reshape(6, 4).astype(np.float64)
+    idx = np.arange(n, dtype=np.uint64)
+    st = rng.Stream(seed, "band")
+    p = st.integers(idx * np.uint64(8), 0, 5)
+    depth = 0.2 + 19.8 * st.uniform(idx * np.uint64(8) + np.uint64(1))
+    half = math.tan(math.radians(30.0))
+    x = st.uniform_range(idx * np.uint64(8) + np.uint64(2), -1.0, 1.0) * depth * half * 16.0 / 9.0
+    y = st.uniform_range(idx * np.uint64(8) + np.uint64(3), -1.0, 1.0) * depth * half
+    pts = np.stack([x, y, -depth], axis=1)
+    nrm, d = planes[p, :3], planes[p, 3]
+    on = pts - nrm * ((nrm * pts).sum(axis=1) + d)[:, None]       # projected onto plane p
+    r = np.exp(-2.0 + 1.5 * st.uniform(idx * np.uint64(8) + np.uint64(4)))
+    t = st.uniform_range(idx * np.uint64(8) + np.uint64(5), -4e-5, 4e-5)
+    c = on + nrm * (t - r)[:, None]
+    local = np.tile(np.eye(4, dtype=np.float32).reshape(1, 16), (n, 1))
+    local[:, 12:15] = c.astype(np.float32)
+    sph = np.zeros((n, 4), np.float32)
+    sph[:, 3] = r.astype(np.float32)
+    ss = st.integers(idx * np.uint64(8) + np.uint64(6), 0, 3)
+    order, offsets = group_by_state_set(ss, 4)
+    G = 16
+    geom = st.integers(idx * np.uint64(8) + np.uint64(7), 0, G - 1).astype(np.uint32)
+    sc = Scene("band", seed, [], [], np.ascontiguousarray(local[order]), None,
+               np.ascontiguousarray(sph[order]), np.ascontiguousarray(geom[order]), offsets,
+               lod_table(np.tile(np.array([[300, 30]]), (G, 1))), 2)
+    sc.views = [view]
+    return sc
+

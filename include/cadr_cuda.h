@@ -368,7 +368,8 @@ CADR_API cadr_status cadr_scene_propagate(cadr_scene* scene, int write_world_sph
  * selects the LOD and compacts visible drawables of StateSet s into
  * cmds[offsets[s] .. offsets[s]+counts[s]) in ascending drawable order.
  * cmds: N records; counts: S words; marginal: optional ceil(N/32) words, bit i
- * set when drawable i lies within the tolerance band of a plane. */
+ * set when the surface of drawable i's world sphere lies within 1e-5 of a
+ * plane, |dist + r| <= 1e-5 in world units (reported, not special-cased). */
 CADR_API cadr_status cadr_cull(cadr_scene* scene, const cadr_view* view,
                                cadr_draw_indexed_cmd* cmds, uint32_t* counts,
                                uint32_t* marginal, cadr_stream stream);

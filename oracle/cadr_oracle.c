@@ -206,7 +206,8 @@ int oracle_propagate(const float* parent_world, uint64_t num_parents, const floa
 /* Plane test, marginal band and LOD of one world sphere (project spec):
  *   dist_p  = ((nx*cx + ny*cy) + nz*cz) + d
  *   visible = dist_p >= -r for all six planes
- *   marginal= |dist_p + r| <= 1e-5 * max(1, |d| + r) for some plane
+ *   marginal= |dist_p + r| <= 1e-5 for some plane: the sphere's surface lies
+ *             within 1e-5 of that plane (an absolute band, in world units)
  *   zc      = perspective ? max(-z_view, near) : 1, z_view = ((vz0*cx+vz1*cy)+vz2*cz)+vz3
  *   lod     = first k < L-1 with r*lod_scale >= T[k]*zc, else L-1 */
 void oracle_classify(const float* ws, const cadr_view* v, uint32_t num_lods, int* visible,
@@ -222,8 +223,7 @@ void oracle_classify(const float* ws, const cadr_view* v, uint32_t num_lods, int
         dist = dist + pl[3];
         if (!(dist >= -r)) vis = 0;
         float t = dist + r;
-        float tol = 1e-5f * fmaxf(1.0f, fabsf(pl[3]) + r);
-        if (fabsf(t) <= tol) mar = 1;
+        if (fabsf(t) <= 1e-5f) mar = 1;
     }
     float zc = 1.0f;
     if (v->perspective) {

@@ -62,6 +62,18 @@ def test_edge_cases_against_oracle(ctx, n, levels, S, lods, empty):
         assert res["counts"][s] == 0
 
 
+def test_marginal_band_against_oracle(ctx):
+    """Spheres placed against the six planes at surface distances around
+    the 1e-5 band: about a quarter are marginal.  Visibility, LOD, every
+    command word and every marginal bit equal the oracle's."""
+    sc = scenes.band_scene(seed=5, n=200_003)
+    res, _, _ = gpu_cull(ctx, sc, want_world=True)
+    ref = bind.cull(sc, sc.views[0], want_world=True)
+    assert_same(res, ref, sc.state_set_offsets)
+    marked = int(np.unpackbits(res["marginal"].view(np.uint8)).sum())
+    assert 0.15 * sc.n < marked < 0.35 * sc.n
+
+
 def test_empty_scene(ctx):
     sc = scenes.small_scene(seed=1, n=0, num_levels=1, num_state_sets=4, num_lods=2)
     ds = lib.DeviceScene(ctx, sc)

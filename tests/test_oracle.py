@@ -251,14 +251,40 @@ def test_cull_known_answers(oracle_lib):
 
 
 def test_marginal_band(oracle_lib):
-    """A sphere touching a plane exactly (dist == -r) is visible and marginal."""
+    """The marginal band is absolute: a sphere is marginal when its surface
+    lies within 1e-5 of a plane, |dist + r| <= 1e-5, whatever the plane's
+    offset.  Near plane at z = -1 (the camera looks down -Z), far plane at
+    z = -100."""
     from oracle import bind
-    # near plane at z = -1 (camera looks down -Z): centre z = -0.5, r = 0.5 -> dist = -0.5 = -r
-    sc = _hand_scene([(0, 0, -0.5), (0, 0, -5)], [0.5, 0.5], [0, 0], 1)
+    centres = [(0, 0, -0.5),         # touches the near plane: dist + r == 0
+               (0, 0, -5),           # well inside
+               (0, 0, -0.500005),    # 5e-6 inside the near-plane band
+               (0, 0, -0.50003),     # 3e-5 from the near plane: outside the band
+               (0, 0, -101.0005)]    # 5e-4 beyond the far plane: outside the band
+    sc = _hand_scene(centres, [0.5, 0.5, 0.5, 0.5, 1.0], [0] * 5, 1)
     o = bind.cull(sc, sc.views[0], threads=1)
-    assert o["counts"].tolist() == [2]
-    assert int(o["marginal"][0]) & 1 == 1
-    assert (int(o["marginal"][0]) >> 1) & 1 == 0
+    m = int(o["marginal"][0])
+    assert [(m >> k) & 1 for k in range(5)] == [1, 0, 1, 0, 0]
+    # Visibility is the plane test alone: the last sphere is culled.
+    assert o["counts"].tolist() == [4]
+
+
+def test_band_scene_marks_spheres_within_the_band(oracle_lib):
+    """On spheres placed against the planes, the oracle's marginal bits are
+    the spheres whose surface is within 1e-5 of a plane: recomputed here in
+    double, every marked sphere is within the band up to float rounding
+    (2e-6 at these depths), and about a quarter of them are marked."""
+    from oracle import bind
+    sc = scenes.band_scene(seed=5, n=20_000)
+    o = bind.cull(sc, sc.views[0], threads=1)
+    marked = np.unpackbits(o["marginal"].view(np.uint8), bitorder="little")[:sc.n].astype(bool)
+    planes = sc.views[0]["planes"].reshape(6, 4).astype(np.float64)
+    c = sc.local[:, 12:15].astype(np.float64)
+    t = c @ planes[:, :3].T + planes[:, 3] + sc.sphere[:, 3:4].astype(np.float64)
+    near = np.abs(t).min(axis=1)
+    assert 0.15 * sc.n < marked.sum() < 0.35 * sc.n
+    assert near[marked].max() <= 1e-5 + 2e-6
+    assert near[~marked].min() >= 1e-5 - 2e-6
 
 
 def test_oracle_rejects_bad_offsets(oracle_lib):
