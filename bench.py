@@ -17,6 +17,13 @@ kernel, the tile scan and the write kernel.
          launching stream; `leaf_stage` gives the same for the three leaf
          launches together
 
+Beside the headline, the same line carries (N=1): `batched` (C4, 256 uneven
+views in one persistent launch against 256 plain passes), `tier_a` (the
+reference shader's pass), `c3` (the deep-hierarchy scene at its full
+4,194,304 drawables, with per-level propagation times), `serving` (C5,
+Poisson requests for 60 s with p50/p99 latency) and `cpu_baseline` (the
+oracle on all host cores and on one, median of 5 passes each).
+
 `--impl reference` times the CPU restatement of the pass (the oracle,
 OpenMP over all host cores) on the same workload: the reference itself has
 no CPU implementation of the pass, and its GPU path (Vulkan shaders) cannot
@@ -51,7 +58,11 @@ def parse():
     ap.add_argument("--n", type=int, default=16_777_216, help="drawables of the C2 scene")
     ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (default: min(steps, 50))")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form (C4) measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form (C4) and Tier A measurements")
+    ap.add_argument("--no-c3", action="store_true", help="skip the deep-hierarchy (C3) measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-form (C5) measurement")
+    ap.add_argument("--plain-duration", type=float, default=10.0,
+                    help="serving: seconds of the request stream the one-request-per-launch loop serves")
     ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a", "batched"])
     ap.add_argument("--batched-tuning", default="", help="batched: block_threads,items_per_thread,ctas_per_sm "
                                                            "instead of the autotuner's pick")
@@ -76,6 +87,14 @@ def measured_peak():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def measured_sm_max_mhz() -> float:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f).get("sm_max_mhz", 2070.0))
+    return 2070.0
 
 
 def committed_traffic(key: str):
@@ -139,6 +158,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def bench_config(sc, world: int) -> dict:
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": f"C2 plain pass, {sc.n} drawables, {sc.num_state_sets} StateSets (Zipf 1.1), levels "
+                        f"{sc.level_sizes}, {sc.num_lods} LODs, seed 1",
+            "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
+def committed_profile_value(name: str, key: str):
+    """A `key: value` figure from a committed ncu summary under profiles/."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
 def leaf_algorithmic_bytes(sc, visible: int) -> int:
     """Compulsory DRAM bytes of the leaf stage: per drawable the local
     matrix (64), parent index (4), local sphere (16), geometry index (4) and
@@ -158,14 +194,100 @@ def stream_algorithmic_bytes(sc) -> int:
     return n * (64 + 4 + 16 + 64) + (n + 7) // 8 + 64 * parents
 
 
+def level_algorithmic_bytes(sc, l: int) -> int:
+    """Internal level l >= 1: local read 64, parent index 4, world write 64
+    per node; every parent's world matrix read once."""
+    return sc.level_sizes[l] * (64 + 4 + 64) + sc.level_sizes[l - 1] * 64
+
+
 def step_algorithmic_bytes(sc, visible: int) -> int:
-    """The whole step: the leaf launch plus every internal level l >= 1
-    (local read 64, parent index 4, world write 64, parents read once)."""
-    b = leaf_algorithmic_bytes(sc, visible)
+    """The whole step: the leaf stage plus every internal level l >= 1."""
+    return leaf_algorithmic_bytes(sc, visible) + sum(level_algorithmic_bytes(sc, l)
+                                                     for l in range(1, len(sc.level_sizes)))
+
+
+def time_plain_pass(ctx, ds, sc, out, steps: int, warmup: int):
+    """K untraced passes timed with CUDA events on the context stream, then
+    K traced passes (frame timing) for the per-kernel and per-level shares.
+    Returns (ms per untraced pass, frames, visible, launches per pass)."""
+    import torch
+    view = sc.views[0]
+    for _ in range(warmup):
+        ds.cull(view, out)
+    ctx.sync()
+    ctx.check_device_error()
+    visible = int(ctx.download(out.counts, np.uint32, (sc.num_state_sets,)).sum())
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.sync()
+    l0 = ctx.launch_count
+    ev0.record(stream)
+    for _ in range(steps):
+        ds.cull(view, out)
+    ev1.record(stream)
+    ctx.sync()
+    launches = (ctx.launch_count - l0) // max(1, steps)
+    ms = ev0.elapsed_time(ev1) / steps
+    ctx.check_device_error()
+    ctx.collect_frame_info(True)
+    for _ in range(steps):
+        ds.cull(view, out)
+    ctx.sync()
+    frames = ctx.frame_infos(with_levels=True)
+    ctx.collect_frame_info(False)
+    ctx.check_device_error()
+    return ms, frames, visible, launches
+
+
+def run_c3(ctx, steps: int, warmup: int, peak: float):
+    """C3, the deep-hierarchy scene at its stated size: 4,194,304 drawables
+    under an 8-level BFS tree (branching U{2..16}), 16 StateSets, 2 LODs.
+    One pass per step as in the headline; per-level propagation times from
+    traced passes; checked in full against the oracle."""
+    from cadr_gb300 import lib, scenes
+    from oracle import bind
+    t0 = time.time()
+    sc = scenes.config3()
+    gen_s = time.time() - t0
+    ds = lib.DeviceScene(ctx, sc)
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    ms, frames, visible, launches = time_plain_pass(ctx, ds, sc, out, steps, warmup)
+    got = out.fetch()
+    ref = bind.cull(sc, sc.views[0], threads=bind.max_threads())
+    same = bool(np.array_equal(got["counts"], ref["counts"]) and np.array_equal(
+        bind.valid_cmds(got["cmds"], got["counts"], sc.state_set_offsets).view(np.uint8),
+        bind.valid_cmds(ref["cmds"], ref["counts"], sc.state_set_offsets).view(np.uint8)) and
+        np.array_equal(got["marginal"], ref["marginal"]))
+    mean = lambda k: float(np.mean([f[k] for f in frames]))
+    prop_ms, leaf_ms, stream_ms = mean(0), mean(1), mean(3)
+    level_ms = [float(np.mean([f[4][l] for f in frames])) for l in range(len(sc.level_sizes) - 1)]
     sizes = sc.level_sizes
+    levels = []
     for l in range(1, len(sizes)):
-        b += sizes[l] * (64 + 4 + 64) + sizes[l - 1] * 64
-    return b
+        b = level_algorithmic_bytes(sc, l)
+        t = level_ms[l - 1]
+        levels.append({"level": l, "nodes": sizes[l], "ms": t, "algorithmic_bytes": b,
+                       "gbs": b / (t / 1e3) / 1e9 if t > 0 else None})
+    step_bytes = step_algorithmic_bytes(sc, visible)
+    stream_bytes = stream_algorithmic_bytes(sc)
+    leaf_bytes = leaf_algorithmic_bytes(sc, visible)
+    return {
+        "workload": f"C3 deep hierarchy, {sc.n} drawables, 16 StateSets, 2 LODs, seed 2, internal levels {sizes}",
+        "internal_nodes": int(sum(sizes)), "ms_per_pass": ms, "gdrawables_per_s": sc.n / (ms / 1e3) / 1e9,
+        "visible_fraction": visible / sc.n, "launches_per_pass": launches,
+        "step": {"algorithmic_bytes": step_bytes, "gbs": step_bytes / (ms / 1e3) / 1e9,
+                 "frac": step_bytes / (ms / 1e3) / 1e9 / peak},
+        "traced": {"propagate_ms": prop_ms, "leaf_ms": leaf_ms, "stream_ms": stream_ms,
+                   "leaf_fraction_of_traced_pass": leaf_ms / (prop_ms + leaf_ms),
+                   "stream_kernel": {"algorithmic_bytes": stream_bytes,
+                                     "frac": stream_bytes / (stream_ms / 1e3) / 1e9 / peak},
+                   "leaf_stage": {"algorithmic_bytes": leaf_bytes,
+                                  "frac": leaf_bytes / (leaf_ms / 1e3) / 1e9 / peak},
+                   "levels": levels,
+                   "level_imbalance": {"largest_over_smallest_nodes": max(sizes[1:]) / min(sizes[1:]),
+                                       "slowest_over_fastest_ms": max(level_ms) / min(level_ms)}},
+        "bit_exact_vs_oracle": same, "scene_generation_s": gen_s,
+    }
 
 
 def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_override: str = ""):
@@ -229,6 +351,21 @@ def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_overr
             bind.valid_cmds(gb["cmds"], gb["counts"], off).view(np.uint8),
             bind.valid_cmds(gp["cmds"], gp["counts"], off).view(np.uint8)))
     view_items = sum(sc.n * len(sc.views) for sc in scs)
+    # Compulsory bytes of one batched launch: every scene's world spheres
+    # and geometry ids once (16 + 4 B per drawable; its 8 views share them),
+    # per view its 20-byte commands.  Tables and scratch are not counted.
+    visible = sum(int(ob.fetch()["counts"].sum()) for _, _, ob in items)
+    batched_bytes = sum(sc.n * 20 for sc in scs) + 20 * visible
+    peak = measured_peak()[0]
+    gbs = batched_bytes / (res["batched"][0] / 1e3) / 1e9
+    # Issue ceiling: 4 warp instructions per cycle per SM at the maximum SM
+    # clock, over the thread instructions per item of the committed ncu
+    # capture of the batched kernel.
+    ipi = committed_profile_value("batched_c4.md", "thread_instructions_per_item")
+    import torch
+    sms, mhz = torch.cuda.get_device_properties(0).multi_processor_count, measured_sm_max_mhz()
+    ceiling = sms * 4 * 32 * mhz * 1e6 / ipi / 1e9 if ipi else None
+    items_rate = view_items / (res["batched"][0] / 1e3) / 1e9
     return {
         "workload": f"C4: {len(items)} views over {len(scs)} scenes of {min(s.n for s in scs)}.."
                     f"{max(s.n for s in scs)} drawables (log-uniform), 4 perspective + 4 ortho cascades each",
@@ -241,6 +378,12 @@ def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_overr
         "tuning": {"block_threads": tuning.block_threads, "items_per_thread": tuning.items_per_thread,
                    "ctas_per_sm": tuning.ctas_per_sm, "autotune_ms": tune_ms},
         "bit_identical": identical,
+        "roofline": {"bound": "issue", "algorithmic_bytes": batched_bytes, "achieved_gbs": gbs,
+                     "frac_of_hbm": gbs / peak, "thread_instructions_per_item": ipi,
+                     "issue_ceiling_gitems_per_s": ceiling,
+                     "frac_of_issue_ceiling": items_rate / ceiling if ceiling else None,
+                     "source": "instructions per item from profiles/batched_c4.md; ceiling = SMs x 4 warp "
+                               "instructions per cycle x 32 threads x max SM clock"},
         "note": "batched: scenes propagated once (world spheres), one persistent launch over (view, tile) "
                 "items from a captured CUDA graph; plain: 256 full passes",
     }
@@ -277,9 +420,14 @@ def run_tier_a(ctx, n: int, steps: int, warmup: int, peak: float):
     same = bool(np.array_equal(ctx.download(ind, np.uint32, (n, 4)), ref_ind) and
                 np.array_equal(ctx.download(ptr, np.uint64, (n, 4)), ref_ptr))
     gbs = n * 148 / (ms / 1e3) / 1e9
+    per = committed_profile_value("process_drawables_level3.md", "dram_bytes_per_drawable")
     out = {"workload": f"{n} drawables, 4,096 geometries, {im.num_handles} handles (level {im.level} tables)",
            "gdrawables_per_s": n / (ms / 1e3) / 1e9, "ms": ms, "algorithmic_bytes_per_drawable": 148,
-           "achieved_gbs": gbs, "frac_of_peak": gbs / peak, "bit_exact_vs_oracle": same}
+           "achieved_gbs": gbs, "frac": gbs / peak, "frac_of_peak": gbs / peak,
+           "traffic": per * n if per else None,
+           "traffic_source": "ncu DRAM bytes per drawable of profiles/process_drawables_level3.md "
+                             "(4,194,304-drawable capture) x drawables",
+           "bit_exact_vs_oracle": same}
     out["pack"] = run_pack(ctx, im, steps, warmup, peak, ms, ref_ind, ref_ptr)
     out["consumer_check"] = run_consumer_check(ctx, steps=max(3, min(steps, 10)), warmup=2)
     return out
@@ -438,21 +586,23 @@ def run_pack(ctx, im, steps: int, warmup: int, peak: float, tier_a_ms: float, re
                                   "slots": "drawable creation order", "bit_exact_vs_oracle": fused_same}}
 
 
-def run_serving(args):
+def measure_serving(ctx, rate: float, duration: float, plain_duration: float, num_scenes: int = 64,
+                    inflight: int = 4) -> dict:
     """Serving form on C5: 64 resident scenes (10,000 .. 8,000,000 drawables,
     log-uniform, built as C2 with seeds 4000+i), a Poisson stream of cull
-    requests (rate --rate, 1-4 views each, random cameras with fovY
-    U[30,90]), continuous batching with a 200 us window; beside it the plain
-    loop that serves one request per launch in arrival order.  Latency is
-    submit -> completion; throughput counts (view, drawable) pairs."""
+    requests (`rate` per second for `duration` seconds, 1-4 views each,
+    random cameras with fovY U[30,90]), continuous batching with a 200 us
+    window; beside it the plain loop that serves one request per launch in
+    arrival order, over the first `plain_duration` seconds of the same
+    stream.  Latency is submit -> completion; throughput counts (view,
+    drawable) pairs.  A sample of served results is compared with the plain
+    pass."""
     import time as _t
-    from cadr_gb300 import build, lib, rng, scenes
+    from cadr_gb300 import lib, rng, scenes
     from oracle import bind
-    build.build()
     t0 = _t.time()
-    scs = scenes.config5_scenes(num_scenes=args.serving_scenes)
+    scs = scenes.config5_scenes(num_scenes=num_scenes)
     gen_s = _t.time() - t0
-    ctx = lib.Context(0)
     dss = [lib.DeviceScene(ctx, sc) for sc in scs]
     for ds in dss:
         ds.propagate(world_spheres=True)
@@ -461,9 +611,9 @@ def run_serving(args):
     # The request stream: exponential inter-arrival times, scene and views
     # drawn from the seeded stream.
     st = rng.Stream(4, "serving.requests")
-    nreq = int(args.rate * args.duration)
+    nreq = int(rate * duration)
     idx = np.arange(nreq, dtype=np.uint64)
-    gaps = -np.log(1.0 - st.uniform(idx * np.uint64(4)))  / args.rate
+    gaps = -np.log(1.0 - st.uniform(idx * np.uint64(4))) / rate
     arrive = np.cumsum(gaps)
     scene_of = st.integers(idx * np.uint64(4) + np.uint64(1), 0, len(scs) - 1)
     nview = st.integers(idx * np.uint64(4) + np.uint64(2), 1, 4)
@@ -476,7 +626,7 @@ def run_serving(args):
                 "gdrawables_per_s": items / wall / 1e9, "wall_s": wall}
 
     # Continuous batching.
-    srv = lib.Server(ctx, max_inflight=args.inflight, max_batch_views=64, window_ns=200_000)
+    srv = lib.Server(ctx, max_inflight=inflight, max_batch_views=64, window_ns=200_000)
     lat, items, sub_t, done = [], 0, {}, 0
     start = _t.perf_counter()
     k = 0
@@ -499,12 +649,11 @@ def run_serving(args):
     batched = summarize(lat, items, wall)
     srv.close()
 
-    # Plain loop: one request per launch, first come first served, over the
-    # first 20 s of the same stream (it falls behind the arrivals, so its
-    # queue grows for as long as it runs).
+    # Plain loop: one request per launch, first come first served (it falls
+    # behind the arrivals, so its queue grows for as long as it runs).
     outs = [lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False) for sc in scs for _ in range(4)]
     lat, items = [], 0
-    nplain = int(min(nreq, args.rate * min(args.duration, 20.0)))
+    nplain = int(min(nreq, rate * min(duration, plain_duration)))
     start = _t.perf_counter()
     for j in range(nplain):
         now = _t.perf_counter() - start
@@ -522,9 +671,9 @@ def run_serving(args):
     wall = _t.perf_counter() - start
     plain = summarize(lat, items, wall)
 
-    # Bit-exactness of served results against the plain pass (sample).
-    srv = lib.Server(ctx, max_inflight=args.inflight, max_batch_views=64, window_ns=200_000)
-    ok = True
+    # Served results against the plain pass of the same scene and view.
+    srv = lib.Server(ctx, max_inflight=inflight, max_batch_views=64, window_ns=200_000)
+    ok, checked = True, 0
     for j in range(0, min(nreq, 64)):
         s = scene_of[j]
         v = pool[view0[j]:view0[j] + 1]
@@ -540,18 +689,55 @@ def run_serving(args):
         ok &= bool(np.array_equal(counts, alone["counts"]) and np.array_equal(
             bind.valid_cmds(cmds, counts, scs[s].state_set_offsets).view(np.uint8),
             bind.valid_cmds(alone["cmds"], alone["counts"], scs[s].state_set_offsets).view(np.uint8)))
+        checked += 1
         srv.release(rid)
     srv.close()
-    line = {
-        "metric": "serving: Gdrawables/s and p50/p99 latency", "form": "serving",
-        "value": batched["gdrawables_per_s"], "unit": "Gdrawables/s", "n_gpus": 1, "higher_is_better": True,
-        "config": {"workload": f"C5: {len(scs)} resident scenes, {sum(s.n for s in scs)} drawables total, "
-                               f"Poisson {args.rate:.0f} req/s for {args.duration:.0f} s, 1-4 views, 200 us window",
-                   "inflight_batches": args.inflight},
-        "continuous_batching": batched, "plain_one_request_per_launch": plain,
-        "served_equals_plain_pass": ok, "scene_generation_s": gen_s, "data": "synthetic",
+    for ds in dss:
+        ds.close()
+    return {
+        "workload": f"C5: {len(scs)} resident scenes, {sum(s.n for s in scs)} drawables total, Poisson "
+                    f"{rate:.0f} req/s for {duration:.0f} s, 1-4 views, 200 us window",
+        "inflight_batches": inflight, "p50_ms": batched["p50_ms"], "p99_ms": batched["p99_ms"],
+        "mean_ms": batched["mean_ms"], "gdrawables_per_s": batched["gdrawables_per_s"],
+        "continuous_batching": batched,
+        "plain_one_request_per_launch": dict(plain, seconds_of_stream=min(duration, plain_duration)),
+        "served_equals_plain": ok, "served_checked": checked, "scene_generation_s": gen_s,
     }
+
+
+def run_serving(args):
+    """`--form serving`: the serving measurement alone, as its own line."""
+    from cadr_gb300 import build, lib
+    build.build()
+    ctx = lib.Context(0)
+    r = measure_serving(ctx, args.rate, args.duration, 20.0, args.serving_scenes, args.inflight)
+    line = {"metric": "serving: Gdrawables/s and p50/p99 latency", "form": "serving",
+            "value": r["gdrawables_per_s"], "unit": "Gdrawables/s", "n_gpus": 1, "higher_is_better": True,
+            "config": {"workload": r["workload"], "inflight_batches": args.inflight}, "data": "synthetic", **r}
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(sc, view, passes: int = 5) -> dict:
+    """The oracle on the full C2 scene: the median of `passes` passes on all
+    host cores (the reported value) and of `passes` single-thread passes."""
+    from oracle import bind
+    import oracle
+    oracle.build(with_ref=False)
+    threads = bind.max_threads()
+
+    def median_s(th):
+        ts = []
+        for _ in range(passes):
+            t = time.perf_counter()
+            bind.cull(sc, view, threads=th)
+            ts.append(time.perf_counter() - t)
+        return float(np.median(ts))
+
+    all_s, one_s = median_s(threads), median_s(1)
+    return {"value": sc.n / all_s / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"full C2 scene ({sc.n} drawables) per pass, median of {passes} passes",
+            "all_cores_ms": all_s * 1e3, "single_thread_ms": one_s * 1e3,
+            "single_thread_value": sc.n / one_s / 1e9}
 
 
 def run_reference(args, sc, world, rank):
@@ -586,8 +772,7 @@ def run_reference(args, sc, world, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"C2 plain pass, {sc.n} drawables, 256 StateSets, 3 LODs, seed 1",
-                   "l2": "inputs larger than L2"},
+        "config": bench_config(sc, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -807,10 +992,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"C2 plain pass, {sc.n} drawables, 256 StateSets (Zipf 1.1), levels "
-                               f"{sc.level_sizes}, 3 LODs, seed 1",
-                   "visible_fraction": visible / sc.n, "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": bench_config(sc, world),
+        "visible_fraction": visible / sc.n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": committed_traffic("stream_kernel_traffic_bytes"),
@@ -840,19 +1023,13 @@ def main():
     if not args.no_batched:
         line["batched"] = run_batched(ctx, steps=max(3, min(args.steps, 20)), warmup=3)
         line["tier_a"] = run_tier_a(ctx, args.n, steps=max(3, min(args.steps, 50)), warmup=3, peak=peak)
+    if not args.no_c3:
+        line["c3"] = run_c3(ctx, steps=max(3, min(args.steps, 50)), warmup=3, peak=peak)
+    if rank == 0 and world == 1 and not args.no_serving:
+        line["serving"] = measure_serving(ctx, args.rate, args.duration, args.plain_duration,
+                                          args.serving_scenes, args.inflight)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle import bind
-        import oracle
-        oracle.build(with_ref=False)
-        threads = bind.max_threads()
-        ts = []
-        for _ in range(3):
-            t2 = time.perf_counter()
-            bind.cull(sc, view, threads=threads)
-            ts.append(time.perf_counter() - t2)
-        cms = float(np.median(ts))
-        line["cpu_baseline"] = {"value": sc.n / cms / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"full C2 scene ({sc.n} drawables), median of 3 passes"}
+        line["cpu_baseline"] = cpu_baseline(sc, view)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -214,9 +214,12 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
     cudaDeviceSynchronize();
     destroy_batched_state(ctx);
     scratch_release(ctx->scratch);
-    for (int f = 0; f < cadr_context::kFrames; f++)
+    for (int f = 0; f < cadr_context::kFrames; f++) {
         for (int k = 0; k < 4; k++)
             if (ctx->frame_ev[f][k]) cudaEventDestroy(ctx->frame_ev[f][k]);
+        for (int k = 0; k < CADR_MAX_LEVELS; k++)
+            if (ctx->level_ev[f][k]) cudaEventDestroy(ctx->level_ev[f][k]);
+    }
     if (ctx->ring) cudaFreeHost(ctx->ring);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     for (int i = 0; i < kRingSlots; i++)
@@ -273,11 +276,16 @@ CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int 
     if (!ctx) return fail(CADR_ERR_INVALID_ARG, "set_collect_frame_info: null context");
     DeviceGuard dg(ctx->device);
     if (on && !ctx->frame_ev[0][0]) {
-        for (int f = 0; f < cadr_context::kFrames; f++)
+        for (int f = 0; f < cadr_context::kFrames; f++) {
             for (int k = 0; k < 4; k++) {
                 cudaError_t e = cudaEventCreate(&ctx->frame_ev[f][k]);
                 if (e != cudaSuccess) return cuda_fail(e, "set_collect_frame_info: events");
             }
+            for (int k = 1; k < CADR_MAX_LEVELS; k++) {
+                cudaError_t e = cudaEventCreate(&ctx->level_ev[f][k]);
+                if (e != cudaSuccess) return cuda_fail(e, "set_collect_frame_info: level events");
+            }
+        }
     }
     ctx->collect_frames = on != 0;
     ctx->frame_tail = ctx->frame_head;
@@ -291,15 +299,21 @@ CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_
     DeviceGuard dg(ctx->device);
     uint32_t k = 0;
     while (k < max_frames && ctx->frame_tail < ctx->frame_head) {
-        cudaEvent_t* ev = ctx->frame_ev[ctx->frame_tail % cadr_context::kFrames];
+        const uint64_t f = ctx->frame_tail % cadr_context::kFrames;
+        cudaEvent_t* ev = ctx->frame_ev[f];
+        cudaEvent_t* lv = ctx->level_ev[f];
         cudaError_t e = cudaEventSynchronize(ev[3]);
         if (e != cudaSuccess) return cuda_fail(e, "get_frame_infos: wait");
         cadr_frame_info& fi = out[k++];
+        fi = cadr_frame_info{};
         fi.frame = ctx->frame_tail;
         cudaEventElapsedTime(&fi.propagate_ms, ev[0], ev[1]);
         cudaEventElapsedTime(&fi.leaf_ms, ev[1], ev[3]);
         cudaEventElapsedTime(&fi.total_ms, ev[0], ev[3]);
         cudaEventElapsedTime(&fi.stream_ms, ev[1], ev[2]);
+        fi.num_levels = ctx->frame_levels[f];
+        for (uint32_t l = 1; l < fi.num_levels; l++)
+            cudaEventElapsedTime(&fi.level_ms[l], l == 1 ? ev[0] : lv[l - 1], lv[l]);
         ctx->frame_tail++;
     }
     *num_frames = k;

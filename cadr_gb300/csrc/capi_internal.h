@@ -41,6 +41,8 @@ struct cadr_context {
     static constexpr int kFrames = 256;
     bool collect_frames = false;
     cudaEvent_t frame_ev[kFrames][4] = {};  // before levels, after levels, after stream kernel, after leaf stage
+    cudaEvent_t level_ev[kFrames][CADR_MAX_LEVELS] = {};  // after level l's propagation (l >= 1)
+    uint32_t frame_levels[kFrames] = {};
     uint64_t frame_head = 0, frame_tail = 0;
 };
 
@@ -77,6 +79,10 @@ cadr_status scene_prepare(cadr_scene* sc, cudaStream_t stream);
 cadr_status scene_mark_read(cadr_scene* sc, cudaStream_t stream);
 ViewConst to_view_const(const cadr_view& v);
 cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, ViewJob* jobs, uint64_t* total);
-cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream);
+// Propagation of the internal levels 1..L-1 on `stream`, each level a
+// programmatic dependent of the one before.  With `level_events`, the
+// event of level l is recorded after its launch and the levels run one
+// after the other (frame timing).
+cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream, cudaEvent_t* level_events = nullptr);
 LeafArgs leaf_args(cadr_scene* sc);
 }  // namespace cadr

@@ -109,7 +109,7 @@ static cadr_status after_upload(cadr_scene* sc)
 }
 
 // Propagation of the internal levels 1..L-1 (level 0's world is its local).
-cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
+cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream, cudaEvent_t* level_events)
 {
     cadr_context* ctx = sc->ctx;
     for (uint32_t l = 1; l < sc->desc.num_levels; l++) {
@@ -117,9 +117,13 @@ cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream)
             reinterpret_cast<const float4*>(sc->buf.level_world[l - 1]), (uint32_t)sc->desc.level_size[l - 1],
             reinterpret_cast<const float4*>(sc->buf.level_local[l]), sc->buf.level_parent[l],
             (uint32_t)sc->desc.level_size[l], reinterpret_cast<float4*>(sc->buf.level_world[l]), 1,
-            ctx->d_error, ctx->spin_limit_ns, stream, l >= 2);
+            ctx->d_error, ctx->spin_limit_ns, stream, l >= 2 && !level_events);
         if (e != cudaSuccess) return cuda_fail(e, "propagate: launch");
         if (sc->desc.level_size[l]) ctx->launches++;
+        if (level_events) {
+            e = cudaEventRecord(level_events[l], stream);
+            if (e != cudaSuccess) return cuda_fail(e, "propagate: level event");
+        }
     }
     return CADR_OK;
 }
@@ -358,12 +362,16 @@ CADR_API cadr_status cadr_cull(cadr_scene* sc, const cadr_view* view, cadr_draw_
         if (e != cudaSuccess) return cuda_fail(e, "cull: order after previous pass");
     }
     cudaEvent_t* fev = nullptr;
+    cudaEvent_t* lev = nullptr;
     if (ctx->collect_frames) {
         if (ctx->frame_head - ctx->frame_tail == (uint64_t)cadr_context::kFrames) ctx->frame_tail++;
-        fev = ctx->frame_ev[ctx->frame_head % cadr_context::kFrames];
+        const uint64_t f = ctx->frame_head % cadr_context::kFrames;
+        fev = ctx->frame_ev[f];
+        lev = ctx->level_ev[f];
+        ctx->frame_levels[f] = sc->desc.num_levels;
         cudaEventRecord(fev[0], s);
     }
-    st = propagate_levels(sc, s);
+    st = propagate_levels(sc, s, lev);
     if (st != CADR_OK) return st;
     if (fev) cudaEventRecord(fev[1], s);
     LeafArgs a = leaf_args(sc);

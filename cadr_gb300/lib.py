@@ -91,7 +91,7 @@ class RequestResult(C.Structure):
 
 class FrameInfo(C.Structure):
     _fields_ = [("frame", u64), ("propagate_ms", C.c_float), ("leaf_ms", C.c_float), ("total_ms", C.c_float),
-                ("stream_ms", C.c_float)]
+                ("stream_ms", C.c_float), ("num_levels", u32), ("level_ms", C.c_float * MAX_LEVELS)]
 
 
 _SIGS = {
@@ -297,13 +297,21 @@ class Context:
     def collect_frame_info(self, on: bool):
         check(self.lib.cadr_context_set_collect_frame_info(self.handle, 1 if on else 0))
 
-    def frame_infos(self):
+    def frame_infos(self, with_levels: bool = False):
+        """Finished frames as (propagate, leaf, total, stream) ms tuples; with
+        with_levels, each tuple ends with the list of per-level times
+        (levels 1..L-1)."""
         buf = (FrameInfo * 256)()
         n = u32()
         out = []
         while True:
             check(self.lib.cadr_context_get_frame_infos(self.handle, buf, 256, C.byref(n)))
-            out += [(buf[i].propagate_ms, buf[i].leaf_ms, buf[i].total_ms, buf[i].stream_ms) for i in range(n.value)]
+            for i in range(n.value):
+                f = buf[i]
+                t = (f.propagate_ms, f.leaf_ms, f.total_ms, f.stream_ms)
+                if with_levels:
+                    t += ([f.level_ms[l] for l in range(1, f.num_levels)],)
+                out.append(t)
             if n.value < 256:
                 return out
 

@@ -429,15 +429,20 @@ CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* tunin
 /* Frame timing, the CUDA counterpart of CadR::FrameInfo's GPU timestamps
  * (src/CadR/FrameInfo.h:15-31, collected in Renderer.cpp:600-702): while
  * collection is on, every plain pass records events before propagation,
- * between propagation and the fused leaf kernel, and after it, into a ring
- * of 256 frames.  get_frame_infos waits for and returns the frames finished
- * since the previous call. */
+ * after each internal level, between propagation and the leaf stage, after
+ * the stream kernel and after the leaf stage, into a ring of 256 frames.
+ * get_frame_infos waits for and returns the frames finished since the
+ * previous call.  A pass with frame timing launches its kernels one after
+ * the other (no programmatic overlap across the recorded events), so its
+ * times are each kernel's own. */
 typedef struct cadr_frame_info {
     uint64_t frame;
     float propagate_ms;     /* internal hierarchy levels */
     float leaf_ms;          /* leaf stage: stream, tile scan and write kernels */
     float total_ms;
     float stream_ms;        /* the leaf stream kernel alone (part of leaf_ms) */
+    uint32_t num_levels;    /* internal levels of the scene */
+    float level_ms[CADR_MAX_LEVELS]; /* level l's propagation (level 0 has none: 0) */
 } cadr_frame_info;
 CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int on);
 CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_info* out,

@@ -52,11 +52,12 @@ def test_struct_layouts_match_header(tmp_path):
 #include <stddef.h>
 #include "cadr_cuda.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",
     sizeof(cadr_draw_indirect_cmd), sizeof(cadr_draw_indexed_cmd), sizeof(cadr_drawable_gpu_data),
     sizeof(cadr_drawable_pointers), sizeof(cadr_lod), sizeof(cadr_view), sizeof(cadr_scene_desc),
     sizeof(cadr_scene_buffers), sizeof(cadr_batch_view), sizeof(cadr_tuning), sizeof(cadr_server_config),
-    sizeof(cadr_request_result), offsetof(cadr_batch_view, cmds));
+    sizeof(cadr_request_result), offsetof(cadr_batch_view, cmds), sizeof(cadr_frame_info),
+    offsetof(cadr_frame_info, level_ms));
   return 0; }
 """)
     exe = tmp_path / "sz"
@@ -64,7 +65,8 @@ int main(void) {
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     want = [16, CMD_DTYPE.itemsize, DRAWABLE_DTYPE.itemsize, 32, LOD_DTYPE.itemsize, VIEW_DTYPE.itemsize,
             C.sizeof(lib.SceneDesc), C.sizeof(lib.SceneBuffers), C.sizeof(lib.BatchView), C.sizeof(lib.Tuning),
-            C.sizeof(lib.ServerConfig), C.sizeof(lib.RequestResult), lib.BatchView.cmds.offset]
+            C.sizeof(lib.ServerConfig), C.sizeof(lib.RequestResult), lib.BatchView.cmds.offset,
+            C.sizeof(lib.FrameInfo), lib.FrameInfo.level_ms.offset]
     assert got == want
     assert got[:6] == [16, 20, 48, 32, 16, 144]
 

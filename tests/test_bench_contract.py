@@ -22,3 +22,8 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] == 3
     assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    # Both arms print the same config dict for the same scene and world size.
+    sys.path.insert(0, ROOT)
+    import bench
+    from cadr_gb300 import scenes
+    assert d["config"] == bench.bench_config(scenes.config2(n=65536), 1)

@@ -107,6 +107,30 @@ def test_c3_deep_hierarchy_against_oracle(ctx):
     assert_same(res, ref, sc.state_set_offsets)
 
 
+def test_c3_full_size_against_oracle(ctx):
+    """The deep-hierarchy scene at its stated size: 4,194,304 drawables
+    under 8 internal levels (branching U{2..16}); counts, every command
+    word, the marginal bitmask and all world matrices compared in full.
+    Frame timing reports one time per propagated level."""
+    sc = scenes.config3()
+    assert sc.n == 4_194_304 and len(sc.level_sizes) == 8
+    ds = lib.DeviceScene(ctx, sc)
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    ctx.collect_frame_info(True)
+    ds.cull(sc.views[0], out)
+    ctx.sync()
+    frames = ctx.frame_infos(with_levels=True)
+    ctx.collect_frame_info(False)
+    ctx.check_device_error()
+    res = out.fetch()
+    res["world"] = ctx.download(ds.buffers().world, np.float32, (sc.n, 16))
+    ref = bind.cull(sc, sc.views[0], threads=bind.max_threads(), want_world=True)
+    assert_same(res, ref, sc.state_set_offsets)
+    assert len(frames) == 1 and len(frames[0][4]) == 7
+    assert all(t > 0 for t in frames[0][4])
+    assert sum(frames[0][4]) <= frames[0][0] * 1.01 + 1e-3
+
+
 def test_c2_full_size_against_oracle(ctx):
     """The headline scene: 16,777,216 drawables, compared in full."""
     sc = scenes.config2()
