@@ -187,6 +187,7 @@ CADR_API cadr_status cadr_context_create(int device, cadr_context** out)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->upload_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->pass_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->shard_counted, cudaEventDisableTiming);
     for (int i = 0; i < kRingSlots && e == cudaSuccess; i++)
         e = cudaEventCreateWithFlags(&ctx->ring_event[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->ring), ctx->ring_bytes, cudaHostAllocDefault);
@@ -214,6 +215,7 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
     cudaDeviceSynchronize();
     destroy_batched_state(ctx);
     scratch_release(ctx->scratch);
+    scratch_release(ctx->shard_scratch);
     for (int f = 0; f < cadr_context::kFrames; f++) {
         for (int k = 0; k < 4; k++)
             if (ctx->frame_ev[f][k]) cudaEventDestroy(ctx->frame_ev[f][k]);
@@ -226,6 +228,7 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
         if (ctx->ring_event[i]) cudaEventDestroy(ctx->ring_event[i]);
     if (ctx->upload_done) cudaEventDestroy(ctx->upload_done);
     if (ctx->pass_done) cudaEventDestroy(ctx->pass_done);
+    if (ctx->shard_counted) cudaEventDestroy(ctx->shard_counted);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->upload_stream) cudaStreamDestroy(ctx->upload_stream);
     delete ctx;

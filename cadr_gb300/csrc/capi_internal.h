@@ -35,6 +35,9 @@ struct cadr_context {
     uint32_t fault = 0;
     std::atomic<uint64_t> launches{0};
     cadr::Scratch scratch;                 // lookback scratch of plain passes
+    cadr::Scratch shard_scratch;           // planes and tile carries kept from a shard's count to its write
+    cudaEvent_t shard_counted = nullptr;   // recorded after a shard's count phase
+    cadr_scene* shard_scene = nullptr;     // the scene whose shard pass awaits its write phase
     cadr_tuning tuning = {256, 4, 4, 0};
     cadr::BatchedState* batched = nullptr;
     // frame timing ring (cadr_frame_info)

@@ -196,6 +196,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// Where a shard of a pass split over several devices puts its commands:
+// the k-th visible drawable of StateSet region s goes to dst_base[s] + k of
+// a merged buffer of `capacity` commands, with firstInstance = its index in
+// the shard + first_instance (its index in the whole scene).
+struct ShardPlacement {
+    const uint32_t* dst_base;
+    uint32_t first_instance;
+    uint32_t capacity;
+};
+
 // ---------------------------------------------------------------------------
 // View constants as the kernels consume them.
 struct ViewConst {

@@ -210,11 +210,13 @@ struct Tile {
     // The commands of the thread's visible items in rows [J0, J1); bit j of
     // vis_bits and ent[j - J0] belong to row j.  A slot outside the n
     // commands (only possible from inconsistent offsets or carries) is
-    // flagged with CADR_DEVERR_BAD_INDEX and not written.
-    template <int J0, int J1>
+    // flagged with CADR_DEVERR_BAD_INDEX and not written.  With kShard the
+    // commands are placed by `sp` instead of at offsets[s] + k.
+    template <int J0, int J1, bool kShard = false>
     __device__ static __forceinline__ void write_cmds(const Smem& sm, uint32_t vis_bits, const uint4 (&ent)[J1 - J0],
                                                       uint32_t b, uint32_t n, const uint32_t* __restrict__ offsets,
-                                                      uint32_t* __restrict__ cmds, uint32_t* error)
+                                                      uint32_t* __restrict__ cmds, uint32_t* error,
+                                                      const ShardPlacement& sp = ShardPlacement{})
     {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
@@ -227,17 +229,19 @@ struct Tile {
             const uint32_t start = (r == rf) ? start_f : offsets[r];
             const uint32_t ei = excl(sm, i - b);
             const uint32_t slot = (start >= b) ? start + (ei - excl(sm, start - b)) : start + carry + ei;
-            if (slot >= n) {
+            uint32_t out = slot;
+            if (kShard) out = (slot < n) ? __ldg(sp.dst_base + r) + (slot - start) : 0xffffffffu;
+            if (slot >= n || (kShard && out >= sp.capacity)) {
                 atomicOr(error, CADR_DEVERR_BAD_INDEX);
                 continue;
             }
             const uint4 e = ent[j - J0];
-            uint32_t* c = cmds + (size_t)slot * 5;
+            uint32_t* c = cmds + (size_t)out * 5;
             c[0] = e.x;
             c[1] = 1u;
             c[2] = e.y;
             c[3] = e.z;
-            c[4] = i;
+            c[4] = kShard ? i + sp.first_instance : i;
         }
     }
 

@@ -291,7 +291,10 @@ constexpr int kWriteCtasPerSm = 6;  // 40 registers; 5 and 8 measured slower
 // but the carry (the planes, the geometry ids, the offsets, the LOD-table
 // gathers) is loaded while the scan still runs, and only the carry is read
 // after griddepcontrol.wait.  The loads are independent of one another,
-// so a tile costs about two memory round trips.
+// so a tile costs about two memory round trips.  With kShard (a shard of a
+// pass split over devices) the commands are placed by a.shard and the
+// counts, written by the region-count kernel before, are left alone.
+template <bool kShard>
 __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kernel(const LeafArgs a)
 {
     __shared__ LeafTile::Smem sm;
@@ -323,7 +326,47 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     if (t == 0) sm.info[2] = load_relaxed_u32(a.tile_words + tile);
     __syncthreads();
     LeafTile::scan(sm, off, a.num_state_sets, b, a.n);
-    LeafTile::write_ent(sm, vis_bits, ent, b, a.n, tile == 0, off, a.num_state_sets, a.cmds, a.counts, a.error);
+    if (kShard)
+        LeafTile::write_cmds<0, kLeafIpt, true>(sm, vis_bits, ent, b, a.n, off, a.cmds, a.error, a.shard);
+    else
+        LeafTile::write_ent(sm, vis_bits, ent, b, a.n, tile == 0, off, a.num_state_sets, a.cmds, a.counts, a.error);
+}
+
+// Sharded pass: the visible drawables of every StateSet region, one warp
+// per region, from the visibility plane and the carries the tile scan left
+// (the carry of a tile counts the visible drawables of the region holding
+// the tile's first drawable that precede the tile).  A region that starts
+// before the tile of its last drawable takes that tile's carry and counts
+// the bits from the tile start; one that starts inside it counts its own
+// bits; either way at most one tile of 2,048 bits is read.
+__global__ void __launch_bounds__(256) leaf_region_count_kernel(const uint32_t* __restrict__ planes,
+                                                                const uint32_t* __restrict__ carries,
+                                                                const uint32_t* __restrict__ offsets, uint32_t S,
+                                                                uint32_t* __restrict__ counts)
+{
+    const uint32_t region = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (region >= S) return;
+    const uint32_t s0 = __ldg(offsets + region), e = __ldg(offsets + region + 1);
+    uint32_t c = 0, base = 0;
+    if (e > s0) {
+        const uint32_t last_tile = (e - 1) / (uint32_t)kLeafTile;
+        const uint32_t tb = last_tile * (uint32_t)kLeafTile;
+        uint32_t from = s0;
+        if (s0 < tb) {
+            from = tb;
+            base = __ldg(carries + last_tile);
+        }
+        for (uint32_t w = (from >> 5) + lane; w <= ((e - 1) >> 5); w += 32u) {
+            uint32_t v = __ldg(planes + w);
+            const uint32_t lo = w * 32u;
+            if (from > lo) v &= ~0u << (from - lo);      // from - lo in 1..31
+            if (e < lo + 32u) v &= (1u << (e - lo)) - 1u;  // e - lo in 1..31
+            c += __popc(v);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(~0u, c, o);
+    if (lane == 0) counts[region] = base + c;
 }
 
 // Internal level propagation.  With `staged`, the CTA's run of parents
@@ -446,8 +489,8 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
-                             bool after_level_kernel)
+cudaError_t launch_leaf_stream_scan(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
+                                    bool after_level_kernel)
 {
     if (a.n == 0) return cudaSuccess;
     const uint32_t tiles = (a.n + kLeafTile - 1) / kLeafTile;
@@ -474,7 +517,25 @@ cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream,
         if (er != cudaSuccess) return er;
     }
     leaf_tile_scan_kernel<<<1, kScanThreads, 0, stream>>>(b.tile_words, tiles);
-    LeafArgs c = b;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_region_counts(const LeafArgs& a, Scratch& s, cudaStream_t stream)
+{
+    if (a.num_state_sets == 0) return cudaSuccess;
+    const uint32_t grid = (a.num_state_sets + 7) / 8;
+    leaf_region_count_kernel<<<grid, 256, 0, stream>>>(s.planes, reinterpret_cast<const uint32_t*>(s.tile_state),
+                                                       a.offsets, a.num_state_sets, a.counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_write(const LeafArgs& a, Scratch& s, cudaStream_t stream, bool after_scan)
+{
+    if (a.n == 0) return cudaSuccess;
+    const uint32_t tiles = (a.n + kLeafTile - 1) / kLeafTile;
+    LeafArgs c = a;
+    c.planes = s.planes;
+    c.tile_words = reinterpret_cast<uint32_t*>(s.tile_state);
     c.off_cap = kWriteOffsetCap;
     const size_t smem = ((a.num_state_sets + 1 <= kWriteOffsetCap) ? a.num_state_sets + 1 : 0) * sizeof(uint32_t);
     cudaLaunchAttribute attr;
@@ -485,10 +546,22 @@ cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream,
     cfg.blockDim = dim3(kLeafThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, leaf_write_kernel, c);
+    cfg.attrs = after_scan ? &attr : nullptr;
+    cfg.numAttrs = after_scan ? 1 : 0;
+    const cudaError_t e = c.shard.dst_base ? cudaLaunchKernelEx(&cfg, leaf_write_kernel<true>, c)
+                                           : cudaLaunchKernelEx(&cfg, leaf_write_kernel<false>, c);
     return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
+                             bool after_level_kernel)
+{
+    if (a.n == 0) return cudaSuccess;
+    const cudaError_t e = launch_leaf_stream_scan(a, s, stream, after_stream, after_level_kernel);
+    if (e != cudaSuccess) return e;
+    LeafArgs c = a;
+    c.shard = ShardPlacement{};
+    return launch_leaf_write(c, s, stream, true);
 }
 
 }  // namespace cadr

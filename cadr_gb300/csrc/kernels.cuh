@@ -41,6 +41,7 @@ struct LeafArgs {
     uint32_t off_cap;             // offsets staged in shared memory when S+1 <= off_cap (set by the launcher)
     uint32_t* planes;             // 3 planes of leaf_plane_stride(N) words: visibility, LOD bits 0, 1 (set by the launcher)
     uint32_t* tile_words;         // one word per leaf tile (set by the launcher)
+    ShardPlacement shard;         // sharded pass: command placement (dst_base null otherwise)
     ViewConst view;
 };
 
@@ -92,6 +93,15 @@ cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 cudaError_t launch_leaf_cull(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
                              bool after_level_kernel = false);
 constexpr uint32_t kLeafCullLaunches = 3;
+
+// The leaf stage in parts, for the sharded pass: the stream kernel and the
+// tile scan (launches 1-2); the per-region visible counts from the planes
+// and the tile carries (one launch, a.counts); the write kernel (launch 3)
+// with the commands placed by a.shard when a.shard.dst_base is set.
+cudaError_t launch_leaf_stream_scan(const LeafArgs& a, Scratch& s, cudaStream_t stream, cudaEvent_t after_stream,
+                                    bool after_level_kernel);
+cudaError_t launch_leaf_region_counts(const LeafArgs& a, Scratch& s, cudaStream_t stream);
+cudaError_t launch_leaf_write(const LeafArgs& a, Scratch& s, cudaStream_t stream, bool after_scan);
 // Words of one bit-plane (one per 32 drawables), padded to 16 bytes.
 __host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 31) / 32 + 3) & ~uint64_t(3); }
 __host__ __device__ constexpr uint64_t leaf_plane_words(uint64_t n) { return 3 * leaf_plane_stride(n); }

@@ -230,6 +230,7 @@ CADR_API cadr_status cadr_scene_destroy(cadr_scene* sc)
 {
     if (!sc) return CADR_OK;
     DeviceGuard dg(sc->ctx->device);
+    if (sc->ctx->shard_scene == sc) sc->ctx->shard_scene = nullptr;
     cudaDeviceSynchronize();
     if (sc->arena) cudaFree(sc->arena);
     if (sc->uploaded) cudaEventDestroy(sc->uploaded);

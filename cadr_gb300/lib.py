@@ -135,6 +135,8 @@ _SIGS = {
     "cadr_scene_propagate": ([vp, i32, vp], i32),
     "cadr_cull": ([vp, vp, vp, vp, vp, vp], i32),
     "cadr_cull_static_scratch": ([vp, vp, vp, vp, vp, vp], i32),
+    "cadr_cull_shard_count": ([vp, vp, vp, vp, vp], i32),
+    "cadr_cull_shard_write": ([vp, vp, u32, vp, u64, vp], i32),
     "cadr_cull_batched": ([vp, C.POINTER(BatchView), u32, C.POINTER(Tuning), i32, vp], i32),
     "cadr_autotune_batched": ([vp, C.POINTER(BatchView), u32, u32, C.POINTER(Tuning),
                                C.POINTER(C.c_float)], i32),

@@ -396,6 +396,34 @@ CADR_API cadr_status cadr_cull_static_scratch(cadr_scene* scene, const cadr_view
                                               cadr_draw_indexed_cmd* cmds, uint32_t* counts,
                                               uint32_t* marginal, cadr_stream stream);
 
+/* Sharded plain pass: one device's part of a pass whose drawables are split
+ * over several devices, as contiguous ranges [lo, hi) of the StateSet-grouped
+ * drawables.  The reference runs the pass on one queue (src/CadR/
+ * Renderer.cpp:108); this is the split of the same pass, so that the merged
+ * output is, word for word, that of cadr_cull on the whole scene.  `scene`
+ * holds the shard: its drawables, the internal levels (replicated), and the
+ * StateSet offsets clipped to the range and taken relative to lo.
+ *
+ * Phase 1, cadr_cull_shard_count: propagation, culling and LOD of the
+ * shard; counts[s] (S words, device) receives its visible drawables in
+ * StateSet region s, marginal (optional) its marginal bits.  The ranks then
+ * exchange their counts (an all-gather of S words: the pass's one exchange
+ * step).  Phase 2, cadr_cull_shard_write: rank r writes its k-th visible
+ * drawable of region s at cmds[dst_base[s] + k] with
+ *   dst_base[s] = offsets[s] + sum_{q < r} count[q][s]
+ * (offsets of the whole scene; dst_base is S words of device memory) and
+ * firstInstance = its index in the shard + first_instance (= lo).  `cmds` is
+ * the merged buffer of cmd_capacity records; a slot outside it is flagged
+ * CADR_DEVERR_BAD_INDEX and not written.  Counts of the merged pass are the
+ * sums over ranks.  The write must follow the count of the same scene on
+ * the same context, with no upload into the scene between them; a second
+ * count replaces a pending one. */
+CADR_API cadr_status cadr_cull_shard_count(cadr_scene* scene, const cadr_view* view, uint32_t* counts,
+                                           uint32_t* marginal, cadr_stream stream);
+CADR_API cadr_status cadr_cull_shard_write(cadr_scene* scene, const uint32_t* dst_base,
+                                           uint32_t first_instance, cadr_draw_indexed_cmd* cmds,
+                                           uint64_t cmd_capacity, cadr_stream stream);
+
 /* Batched form: many (scene, view) pairs culled by one persistent launch over
  * (view, tile) work items, replayed from a captured CUDA graph when the
  * same batch shape repeats.  Scenes must have been propagated with
