@@ -10,7 +10,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "capi_internal.h"
@@ -366,54 +368,105 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
 
 // Autotuner: times every supported (block, items per thread, CTAs per SM)
 // combination on the given batch with CUDA events (median of `reps` runs
-// after one warm-up) and keeps the fastest in the context.
+// after one warm-up) and keeps the fastest in the context.  With a tuning
+// cache set on the context, a batch whose key (batch shape, GPU, driver) is
+// in the cache takes the stored pick without timing anything.
+namespace {
+
+struct TimeBatch {
+    cadr_context* ctx;
+    const cadr_batch_view* views;
+    uint32_t num_views;
+    uint32_t reps;
+    cudaEvent_t a, b;
+};
+
+cadr_status time_batch(const cadr_tuning* tu, void* user, float* out_ms)
+{
+    TimeBatch& T = *static_cast<TimeBatch*>(user);
+    cudaStream_t s = T.ctx->stream;
+    std::vector<float> ts;
+    for (uint32_t r = 0; r <= T.reps; r++) {
+        cudaEventRecord(T.a, s);
+        const cadr_status st = cadr_cull_batched(T.ctx, T.views, T.num_views, tu, 0, s);
+        cudaEventRecord(T.b, s);
+        if (st != CADR_OK) return st;
+        const cudaError_t e = cudaEventSynchronize(T.b);
+        if (e != cudaSuccess) return cuda_fail(e, "autotune: wait");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, T.a, T.b);
+        if (r) ts.push_back(ms);
+    }
+    std::sort(ts.begin(), ts.end());
+    *out_ms = ts[ts.size() / 2];
+    return CADR_OK;
+}
+
+// The cache key of a batch: the GPU (name, SMs, compute capability), the
+// driver, this library's ABI, and the batch's shape (per view: the scene's
+// drawables, StateSets and LODs), the shape hashed with FNV-1a.
+std::string tuning_key(const cadr_context* ctx, const cadr_batch_view* views, uint32_t n)
+{
+    cudaDeviceProp p{};
+    cudaGetDeviceProperties(&p, ctx->device);
+    int driver = 0;
+    cudaDriverGetVersion(&driver);
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int k = 0; k < 8; k++) {
+            h ^= (v >> (8 * k)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    };
+    uint64_t drawables = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        const cadr_scene_desc& d = views[v].scene->desc;
+        mix(d.num_drawables);
+        mix(d.num_state_sets);
+        mix(d.num_lods);
+        drawables += d.num_drawables;
+    }
+    std::string name;
+    for (const char* c = p.name; *c; c++) name += (*c == '"' || *c == '\\') ? '_' : *c;
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s|sms=%d|cc=%d.%d|driver=%d|abi=%d|views=%u|drawables=%llu|shape=%016llx",
+                  name.c_str(), p.multiProcessorCount, p.major, p.minor, driver, cadr_abi_version(), n,
+                  (unsigned long long)drawables, (unsigned long long)h);
+    return buf;
+}
+
+}  // namespace
+
+CADR_API cadr_status cadr_context_set_tuning_cache(cadr_context* ctx, const char* path)
+{
+    if (!ctx) return fail(CADR_ERR_INVALID_ARG, "set_tuning_cache: null context");
+    ctx->tuning_cache = path ? path : "";
+    return CADR_OK;
+}
+
 CADR_API cadr_status cadr_autotune_batched(cadr_context* ctx, const cadr_batch_view* views, uint32_t num_views,
                                            uint32_t reps, cadr_tuning* best, float* best_ms)
 {
     if (!ctx || !views || num_views == 0 || !best) return fail(CADR_ERR_INVALID_ARG, "autotune: bad argument");
     DeviceGuard dg(ctx->device);
-    if (reps == 0) reps = 5;
-    const uint32_t threads[] = {128, 256, 512};
-    const uint32_t ipts[] = {4, 8, 16};
-    const uint32_t ctas[] = {2, 4, 8};
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    cudaStream_t s = ctx->stream;
-    float best_t = 1e30f;
-    cadr_tuning best_tu = ctx->tuning;
-    for (uint32_t th : threads)
-        for (uint32_t ipt : ipts)
-            for (uint32_t c : ctas) {
-                if (th * c > 2048) continue;  // more threads per SM than the hardware holds
-                cadr_tuning tu = {th, ipt, c, 0};
-                std::vector<float> ts;
-                for (uint32_t r = 0; r <= reps; r++) {
-                    cudaEventRecord(a, s);
-                    cadr_status st = cadr_cull_batched(ctx, views, num_views, &tu, 0, s);
-                    cudaEventRecord(b, s);
-                    if (st != CADR_OK) {
-                        cudaEventDestroy(a);
-                        cudaEventDestroy(b);
-                        return st;
-                    }
-                    cudaEventSynchronize(b);
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, a, b);
-                    if (r) ts.push_back(ms);
-                }
-                std::sort(ts.begin(), ts.end());
-                const float med = ts[ts.size() / 2];
-                if (med < best_t) {
-                    best_t = med;
-                    best_tu = tu;
-                }
-            }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    ctx->tuning = best_tu;
-    *best = best_tu;
-    if (best_ms) *best_ms = best_t;
+    for (uint32_t v = 0; v < num_views; v++)
+        if (!views[v].scene) return fail(CADR_ERR_INVALID_ARG, "autotune: view %u has no scene", v);
+    TimeBatch T{ctx, views, num_views, reps ? reps : 5u, nullptr, nullptr};
+    cudaError_t e = cudaEventCreate(&T.a);
+    if (e == cudaSuccess) e = cudaEventCreate(&T.b);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune: events");
+    const std::string key = tuning_key(ctx, views, num_views);
+    cadr_tuning pick = ctx->tuning;
+    float ms = 0;
+    const cadr_status st = cadr_autotune_with(ctx->tuning_cache.empty() ? nullptr : ctx->tuning_cache.c_str(),
+                                              key.c_str(), time_batch, &T, &pick, &ms, nullptr);
+    cudaEventDestroy(T.a);
+    cudaEventDestroy(T.b);
+    if (st != CADR_OK) return st;
+    if (!tuning_valid(pick)) return fail(CADR_ERR_INVALID_ARG, "autotune: cached tuning is not supported");
+    ctx->tuning = pick;
+    *best = pick;
+    if (best_ms) *best_ms = ms;
     return CADR_OK;
 }
 

@@ -39,6 +39,7 @@ struct cadr_context {
     cudaEvent_t shard_counted = nullptr;   // recorded after a shard's count phase
     cadr_scene* shard_scene = nullptr;     // the scene whose shard pass awaits its write phase
     cadr_tuning tuning = {256, 4, 4, 0};
+    std::string tuning_cache;              // autotuner cache file ("" = none)
     cadr::BatchedState* batched = nullptr;
     // frame timing ring (cadr_frame_info)
     static constexpr int kFrames = 256;

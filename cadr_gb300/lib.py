@@ -141,6 +141,11 @@ _SIGS = {
     "cadr_autotune_batched": ([vp, C.POINTER(BatchView), u32, u32, C.POINTER(Tuning),
                                C.POINTER(C.c_float)], i32),
     "cadr_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+    "cadr_context_set_tuning_cache": ([vp, C.c_char_p], i32),
+    "cadr_autotune_with": ([C.c_char_p, C.c_char_p, vp, vp, C.POINTER(Tuning), C.POINTER(C.c_float),
+                            C.POINTER(i32)], i32),
+    "cadr_tuning_cache_lookup": ([C.c_char_p, C.c_char_p, C.POINTER(Tuning), C.POINTER(C.c_float)], i32),
+    "cadr_tuning_cache_store": ([C.c_char_p, C.c_char_p, C.POINTER(Tuning), C.c_float], i32),
     "cadr_set_tuning": ([vp, C.POINTER(Tuning)], i32),
     "cadr_pack_create": ([vp, u32, C.POINTER(vp)], i32),
     "cadr_pack_destroy": ([vp], i32),
@@ -497,6 +502,27 @@ def batch_views(items) -> C.Array:
 def cull_batched(ctx: Context, arr, tuning: Tuning | None = None, use_graph: bool = True, stream=None):
     check(ctx.lib.cadr_cull_batched(ctx.handle, arr, len(arr), C.byref(tuning) if tuning else None,
                                     1 if use_graph else 0, stream))
+
+
+# cadr_time_tuning_fn: (const cadr_tuning*, void* user, float* ms) -> cadr_status
+TIME_TUNING_FN = C.CFUNCTYPE(i32, C.POINTER(Tuning), vp, C.POINTER(C.c_float))
+
+
+def autotune_with(cache_path, key: str, time_fn):
+    """The autotuner's search without a GPU: time_fn(Tuning) -> ms.  Returns
+    (best Tuning, its ms, whether it came from the cache)."""
+    def cb(tp, user, ms_out):
+        ms_out[0] = float(time_fn(tp.contents))
+        return OK
+    fn = TIME_TUNING_FN(cb)
+    best, ms, hit = Tuning(), C.c_float(), i32()
+    check(load().cadr_autotune_with(cache_path.encode() if cache_path else None, key.encode(),
+                                    C.cast(fn, vp), None, C.byref(best), C.byref(ms), C.byref(hit)))
+    return best, ms.value, bool(hit.value)
+
+
+def set_tuning_cache(ctx: Context, path):
+    check(ctx.lib.cadr_context_set_tuning_cache(ctx.handle, path.encode() if path else None))
 
 
 def autotune_batched(ctx: Context, arr, reps: int = 5):

@@ -447,10 +447,30 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
                                        uint32_t num_views, const cadr_tuning* tuning,
                                        int use_graph, cadr_stream stream);
 /* Autotuner: times every supported tuning on this batch (CUDA events, median
- * of `reps` runs) and keeps the fastest as the context's default. */
+ * of `reps` runs) and keeps the fastest as the context's default.  With a
+ * tuning cache set (cadr_context_set_tuning_cache), the pick is stored under
+ * a key of the batch's shape (per view: the scene's drawables, StateSets and
+ * LODs), the GPU (name, SMs, compute capability) and the driver version, and
+ * a later batch with the same key takes it from the cache without timing.
+ * The reference has no tuner: its dispatch shape is fixed (Renderer.cpp:684-692). */
 CADR_API cadr_status cadr_autotune_batched(cadr_context* ctx, const cadr_batch_view* views,
                                            uint32_t num_views, uint32_t reps, cadr_tuning* best,
                                            float* best_ms);
+/* The cache file of the context's autotuner (NULL or "" = no cache). */
+CADR_API cadr_status cadr_context_set_tuning_cache(cadr_context* ctx, const char* path);
+/* The search and the cache without a GPU: cadr_autotune_with times every
+ * supported tuning with time_fn (which returns CADR_OK and the time of one
+ * tuning in *ms) and keeps the fastest; with cache_path set it first looks
+ * `key` up there (then *from_cache = 1 and time_fn is not called) and stores
+ * its pick afterwards.  cadr_tuning_cache_lookup returns CADR_ERR_NOT_READY
+ * when the key is absent.  Keys may not hold quotes, backslashes or line
+ * breaks. */
+typedef cadr_status (*cadr_time_tuning_fn)(const cadr_tuning* tuning, void* user, float* ms);
+CADR_API cadr_status cadr_autotune_with(const char* cache_path, const char* key, cadr_time_tuning_fn time_fn,
+                                        void* user, cadr_tuning* best, float* best_ms, int* from_cache);
+CADR_API cadr_status cadr_tuning_cache_lookup(const char* path, const char* key, cadr_tuning* out, float* ms);
+CADR_API cadr_status cadr_tuning_cache_store(const char* path, const char* key, const cadr_tuning* tuning,
+                                             float ms);
 CADR_API cadr_status cadr_get_tuning(cadr_context* ctx, cadr_tuning* out);
 CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* tuning);
 

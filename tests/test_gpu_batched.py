@@ -76,3 +76,50 @@ def test_autotune_picks_a_supported_tuning(ctx, c4_small):
              for v in sc.views[:2]]
     t, ms = lib.autotune_batched(ctx, lib.batch_views(items), reps=2)
     assert t.block_threads in (128, 256, 512) and t.items_per_thread in (4, 8, 16) and ms > 0
+
+
+def test_autotune_cache_skips_timing_and_gives_identical_output(ctx, c4_small, tmp_path):
+    """With a tuning cache, the second autotune of the same batch shape
+    launches nothing and returns the stored pick; the batch culled with it
+    equals the plain passes."""
+    scs, dss = c4_small
+    items, outs = [], []
+    for sc, ds in zip(scs, dss):
+        for v in sc.views[:3]:
+            o = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+            items.append((ds, v, o))
+            outs.append((sc, ds, v, o))
+    arr = lib.batch_views(items)
+    lib.set_tuning_cache(ctx, str(tmp_path / "tuning.json"))
+    try:
+        l0 = ctx.launch_count
+        t1, ms1 = lib.autotune_batched(ctx, arr, reps=2)
+        l1 = ctx.launch_count
+        assert l1 - l0 >= 24 * 3
+        t2, ms2 = lib.autotune_batched(ctx, arr, reps=2)
+        assert ctx.launch_count == l1
+        assert (t2.block_threads, t2.items_per_thread, t2.ctas_per_sm) == (t1.block_threads, t1.items_per_thread,
+                                                                           t1.ctas_per_sm)
+        assert abs(ms2 - ms1) < 1e-3
+    finally:
+        lib.set_tuning_cache(ctx, None)
+    lib.cull_batched(ctx, arr, t2, use_graph=True)
+    ctx.sync()
+    ctx.check_device_error()
+    for sc, ds, v, o in outs:
+        assert_same(o.fetch(), _plain(ctx, sc, ds, v), sc.state_set_offsets)
+
+
+def test_batched_marginal_bits_equal_plain(ctx):
+    """Spheres against the planes (about a quarter inside the 1e-5 band):
+    the batched form's marginal bits equal the plain pass's."""
+    sc = scenes.band_scene(seed=13, n=150_001)
+    ds = lib.DeviceScene(ctx, sc)
+    ds.propagate(world_spheres=True)
+    o = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    lib.cull_batched(ctx, lib.batch_views([(ds, sc.views[0], o)]), None, use_graph=False)
+    ctx.sync()
+    ctx.check_device_error()
+    got, ref = o.fetch(), _plain(ctx, sc, ds, sc.views[0])
+    assert_same(got, ref, sc.state_set_offsets)
+    assert np.unpackbits(got["marginal"].view(np.uint8)).sum() > 0.15 * sc.n
