@@ -454,7 +454,102 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
     st_f8(wp + 2, mat_col(p0, p1, p2, p3, l2), mat_col(p0, p1, p2, p3, l3));
 }
 
+constexpr int kFoldThreads = 1024;
+
+__host__ __device__ constexpr uint32_t pad16_words(uint32_t n) { return (n + 3u) & ~3u; }
+
+// Shared memory of the folded levels at their maximum: 64 B per node (level
+// 0 and every folded level), the parent indices of the folded levels
+// (each level padded to 16 bytes).
+constexpr size_t kFoldSmemBytes = kFoldMaxNodes * 64 + (kFoldMaxNodes + 4 * CADR_MAX_LEVELS) * 4;
+
+__global__ void __launch_bounds__(kFoldThreads) propagate_small_levels_kernel(const FoldArgs a)
+{
+    extern __shared__ __align__(128) float4 s_mat[];  // level 0, then each folded level: 4 float4 per node
+    __shared__ __align__(8) uint64_t s_bar;
+    // The next level kernel (or the stream kernel) may launch now: it reads
+    // these levels' world matrices only after griddepcontrol.wait.
+    grid_dependents_launch();
+    uint32_t total = a.n0, par_words = 0;
+    for (uint32_t l = 0; l < a.count; l++) {
+        total += a.lvl[l].n;
+        par_words += pad16_words(a.lvl[l].n);
+    }
+    uint32_t* s_par = reinterpret_cast<uint32_t*>(s_mat + 4 * (size_t)total);
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_arrive_expect_tx(&s_bar, total * 64u + par_words * 4u);
+        bulk_copy_g2s(s_mat, a.world0, a.n0 * 64u, &s_bar);
+        uint32_t m = a.n0, po = 0;
+        for (uint32_t l = 0; l < a.count; l++) {
+            const uint32_t n = a.lvl[l].n;
+            bulk_copy_g2s(s_mat + 4 * (size_t)m, a.lvl[l].local, n * 64u, &s_bar);
+            // Padded to 16 bytes: the arena rounds every array up to 256.
+            bulk_copy_g2s(s_par + po, a.lvl[l].parent, pad16_words(n) * 4u, &s_bar);
+            m += n;
+            po += pad16_words(n);
+        }
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&s_bar, 0, a.limit_ns);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            atomicOr(a.error, CADR_DEVERR_MBARRIER_TIMEOUT);
+            mbar_wait_bounded(&s_bar, 0, a.limit_ns);  // let in-flight copies land before exit
+        }
+        return;
+    }
+    uint32_t prev = 0, np = a.n0, m = a.n0, po = 0;
+    for (uint32_t l = 0; l < a.count; l++) {
+        const uint32_t n = a.lvl[l].n;
+        float4* world = a.lvl[l].world;
+        for (uint32_t i = threadIdx.x; i < n; i += kFoldThreads) {
+            uint32_t p = s_par[po + i];
+            if (p >= np) {
+                atomicOr(a.error, CADR_DEVERR_BAD_INDEX);
+                p = 0;
+            }
+            const float4* P = s_mat + 4 * (size_t)(prev + p);
+            float4* C = s_mat + 4 * (size_t)(m + i);
+            const float4 p0 = P[0], p1 = P[1], p2 = P[2], p3 = P[3];
+            const float4 w0 = mat_col(p0, p1, p2, p3, C[0]), w1 = mat_col(p0, p1, p2, p3, C[1]);
+            const float4 w2 = mat_col(p0, p1, p2, p3, C[2]), w3 = mat_col(p0, p1, p2, p3, C[3]);
+            C[0] = w0;
+            C[1] = w1;
+            C[2] = w2;
+            C[3] = w3;
+            st_f8(world + 4 * (size_t)i, w0, w1);
+            st_f8(world + 4 * (size_t)i + 2, w2, w3);
+        }
+        __syncthreads();
+        prev = m;
+        np = n;
+        m += n;
+        po += pad16_words(n);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_small_levels(const FoldArgs& a, cudaStream_t stream)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(propagate_small_levels_kernel,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFoldSmemBytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    uint32_t total = a.n0, par_words = 0;
+    for (uint32_t l = 0; l < a.count; l++) {
+        total += a.lvl[l].n;
+        par_words += pad16_words(a.lvl[l].n);
+    }
+    if (total > kFoldMaxNodes) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)total * 64 + (size_t)par_words * 4;
+    propagate_small_levels_kernel<<<1, kFoldThreads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, const float4* local,
                              const uint32_t* parent, uint32_t n, float4* world, int staged,

@@ -79,6 +79,30 @@ cudaError_t launch_propagate(const float4* parent_world, uint32_t num_parents, c
                              uint32_t* error, uint64_t spin_limit_ns, cudaStream_t stream,
                              bool after_level_kernel = false);
 
+// The leading internal levels of a deep hierarchy, folded into one launch:
+// levels 1..count whose nodes, with level 0's, number at most
+// kFoldMaxNodes.  One CTA bulk-copies all their local matrices, parent
+// indices and level 0's world matrices into shared memory and propagates
+// level after level there, separated by CTA barriers instead of one grid
+// dependency per level.
+constexpr uint32_t kFoldMaxNodes = 3072;
+struct FoldLevel {
+    const float4* local;
+    const uint32_t* parent;
+    float4* world;
+    uint32_t n;
+    uint32_t pad;
+};
+struct FoldArgs {
+    const float4* world0;         // level 0 (world = local)
+    uint32_t n0;
+    uint32_t count;               // folded levels: 1..count
+    FoldLevel lvl[CADR_MAX_LEVELS - 1];
+    uint32_t* error;
+    uint64_t limit_ns;
+};
+cudaError_t launch_small_levels(const FoldArgs& a, cudaStream_t stream);
+
 // Leaf level propagation (+ optional world spheres) without culling.
 cudaError_t launch_leaf_propagate(const LeafArgs& a, cudaStream_t stream);
 

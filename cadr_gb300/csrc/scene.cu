@@ -112,7 +112,39 @@ static cadr_status after_upload(cadr_scene* sc)
 cadr_status propagate_levels(cadr_scene* sc, cudaStream_t stream, cudaEvent_t* level_events)
 {
     cadr_context* ctx = sc->ctx;
-    for (uint32_t l = 1; l < sc->desc.num_levels; l++) {
+    const cadr_scene_desc& d = sc->desc;
+    // Leading levels small enough to hold in one CTA's shared memory (two
+    // at least) are folded into one launch.
+    uint32_t fold = 0;
+    if (d.num_levels >= 3) {
+        uint64_t nodes = d.level_size[0];
+        while (1 + fold < d.num_levels && nodes + d.level_size[1 + fold] <= kFoldMaxNodes)
+            nodes += d.level_size[1 + fold++];
+        if (fold < 2) fold = 0;
+    }
+    if (fold) {
+        FoldArgs f{};
+        f.world0 = reinterpret_cast<const float4*>(sc->buf.level_world[0]);
+        f.n0 = (uint32_t)d.level_size[0];
+        f.count = fold;
+        for (uint32_t k = 0; k < fold; k++) {
+            f.lvl[k].local = reinterpret_cast<const float4*>(sc->buf.level_local[1 + k]);
+            f.lvl[k].parent = sc->buf.level_parent[1 + k];
+            f.lvl[k].world = reinterpret_cast<float4*>(sc->buf.level_world[1 + k]);
+            f.lvl[k].n = (uint32_t)d.level_size[1 + k];
+        }
+        f.error = ctx->d_error;
+        f.limit_ns = ctx->spin_limit_ns;
+        cudaError_t e = launch_small_levels(f, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "propagate: launch folded levels");
+        ctx->launches++;
+        // Frame timing gives the folded launch to its first level.
+        for (uint32_t k = 0; level_events && k < fold; k++) {
+            e = cudaEventRecord(level_events[1 + k], stream);
+            if (e != cudaSuccess) return cuda_fail(e, "propagate: level event");
+        }
+    }
+    for (uint32_t l = 1 + fold; l < d.num_levels; l++) {
         cudaError_t e = launch_propagate(
             reinterpret_cast<const float4*>(sc->buf.level_world[l - 1]), (uint32_t)sc->desc.level_size[l - 1],
             reinterpret_cast<const float4*>(sc->buf.level_local[l]), sc->buf.level_parent[l],

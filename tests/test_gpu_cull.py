@@ -126,9 +126,50 @@ def test_c3_full_size_against_oracle(ctx):
     res["world"] = ctx.download(ds.buffers().world, np.float32, (sc.n, 16))
     ref = bind.cull(sc, sc.views[0], threads=bind.max_threads(), want_world=True)
     assert_same(res, ref, sc.state_set_offsets)
-    assert len(frames) == 1 and len(frames[0][4]) == 7
-    assert all(t > 0 for t in frames[0][4])
-    assert sum(frames[0][4]) <= frames[0][0] * 1.01 + 1e-3
+    # Levels 1-4 (2 + 24 + 216 + 1,982 nodes, with level 0's one node under
+    # the 3,072 of one CTA's shared memory) run folded in one launch, whose
+    # time frame timing gives to level 1.
+    lv = frames[0][4]
+    assert len(frames) == 1 and len(lv) == 7
+    assert lv[0] > 0 and all(t >= 0 for t in lv) and all(t > 0 for t in lv[4:])
+    assert sum(lv) <= frames[0][0] * 1.01 + 1e-3
+    assert ctx.launch_count > 0
+
+
+@pytest.mark.parametrize("n,levels,fanout", [
+    (40_000, 6, 4),    # levels 1-3 folded (with level 0: 9 + 39 + 156 + 625 nodes), 4-5 launched one by one
+    (3_000, 5, 3),     # every internal level folded
+    (200_000, 8, 3),   # folded, then four level kernels
+])
+def test_folded_levels_against_oracle(ctx, n, levels, fanout):
+    sc = scenes.small_scene(seed=n + levels, n=n, num_levels=levels, num_state_sets=7, num_lods=3, fanout=fanout)
+    res, ds, _ = gpu_cull(ctx, sc, want_world=True)
+    ref = bind.cull(sc, sc.views[0], want_world=True)
+    assert_same(res, ref, sc.state_set_offsets)
+    # Every level's world matrices, folded or not: level l from the GPU's
+    # level l-1 by the oracle's product (the first 4,096 nodes per level).
+    b = ds.buffers()
+    prev = None
+    for l, (loc, par) in enumerate(zip(sc.level_local, sc.level_parent)):
+        got = ctx.download(b.level_world[l], np.float32, loc.shape)
+        if l:
+            k = min(len(par), 4096)
+            want = np.stack([bind.mat4_mul(prev[int(par[i])], loc[i]) for i in range(k)])
+            assert np.array_equal(bits(got[:k]), bits(want)), l
+        prev = got
+    assert ctx.check_device_error() == 0
+
+
+def test_bad_parent_in_a_folded_level_is_reported(ctx):
+    sc = scenes.small_scene(seed=4, n=3_000, num_levels=5, num_state_sets=3, fanout=3)
+    sc.level_parent = list(sc.level_parent)
+    sc.level_parent[2] = sc.level_parent[2].copy()
+    sc.level_parent[2][1] = 1_000_000
+    ds = lib.DeviceScene(ctx, sc)
+    out = lib.CullOutputs(ctx, sc.n, sc.num_state_sets)
+    ds.cull(sc.views[0], out)
+    st, bits_ = ctx.device_error_status()
+    assert st == lib.DEVICE and bits_ & 0x4
 
 
 def test_c2_full_size_against_oracle(ctx):
