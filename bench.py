@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form (C5) measurement")
     ap.add_argument("--plain-duration", type=float, default=10.0,
                     help="serving: seconds of the request stream the one-request-per-launch loop serves")
-    ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a", "batched"])
+    ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a", "batched", "c3"])
     ap.add_argument("--batched-tuning", default="", help="batched: block_threads,items_per_thread,ctas_per_sm "
                                                            "instead of the autotuner's pick")
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
@@ -797,6 +797,14 @@ def main():
         print(json.dumps({"form": "batched", **run_batched(ctx, steps=args.steps, warmup=args.warmup,
                                                            tuning_override=args.batched_tuning)}))
         return
+    if args.form == "c3":
+        from cadr_gb300 import build, lib
+        build.build()
+        import oracle
+        oracle.build(with_ref=False)
+        ctx = lib.Context(local)
+        print(json.dumps({"form": "c3", **run_c3(ctx, args.steps, args.warmup, measured_peak()[0])}))
+        return
     if args.form == "tier-a":
         from cadr_gb300 import build, lib
         build.build()
@@ -926,18 +934,19 @@ def main():
         lib.check(L.cadr_download(ctx.handle, h_counts[j].ptr, outs[j].counts.ptr, sc.num_state_sets * 4, None))
         counts_ready[j].record(cstream)
 
+    import ctypes
+    offs_u32 = np.ascontiguousarray(sc.state_set_offsets, np.uint32)
+    host_issue = [0.0]
+
     def e2e_readback(k):
         j = k % 2
         counts_ready[j].synchronize()
-        cnt = h_counts[j].view(np.uint32, (sc.num_state_sets,))
-        d2h = sc.num_state_sets * 4
-        for s in range(sc.num_state_sets):
-            c = int(cnt[s])
-            if c:
-                lib.check(L.cadr_download(ctx.handle, h_cmds[j].ptr + int(offs[s]) * 20,
-                                          outs[j].cmds.ptr + int(offs[s]) * 20, c * 20, None))
-                d2h += c * 20
-        return d2h
+        t = time.perf_counter()
+        nbytes = ctypes.c_uint64()
+        lib.check(L.cadr_download_commands(ctx.handle, h_cmds[j].ptr, outs[j].cmds.ptr, h_counts[j].ptr,
+                                           offs_u32.ctypes.data, sc.num_state_sets, ctypes.byref(nbytes), None))
+        host_issue[0] += time.perf_counter() - t
+        return sc.num_state_sets * 4 + nbytes.value
 
     def e2e_run(steps):
         d2h = 0
@@ -952,9 +961,11 @@ def main():
 
     e2e_run(3)
     barrier()
+    host_issue[0] = 0.0
     t1 = time.perf_counter()
     d2h_total = e2e_run(e2e_steps)
     e2e_s = (time.perf_counter() - t1) / e2e_steps
+    readback_issue_ms = host_issue[0] / e2e_steps * 1e3
     barrier()
     # The last step's read-back equals the device-resident pass's result.
     j = (e2e_steps - 1) % 2
@@ -1013,6 +1024,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h_total // max(1, e2e_steps), "ms_per_step": e2e_s * 1e3,
                 "upload_only_ms_per_step": upload_only_s * 1e3,
+                "readback_issue_host_ms_per_step": readback_issue_ms,
                 "host_link_h2d_gbs": h2d / upload_only_s / 1e9,
                 "pipelining": "two device scenes alternate; a step's uploads overlap the previous step's pass and read-back",
                 "readback_equals_device_pass": e2e_same},

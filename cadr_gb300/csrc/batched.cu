@@ -84,8 +84,11 @@ __device__ __forceinline__ void copy_job(const ViewJob* __restrict__ src, ViewJo
 // record and the staged StateSet offsets (switched when the job changes),
 // so item k+1's ballots and job never overwrite what item k's write phase
 // reads: three CTA barriers per item.  The next item is taken by the first
-// thread of warp 1 (warp 0 does the lookback) before the carry barrier,
-// which also publishes it.
+// thread of warp 1 (warp 0 does the lookback) when the current one starts,
+// and published with its job by the carry barrier.  A CTA thus holds one
+// item it has not started; every wait still ends, since the smallest
+// unpublished item is always one a CTA is working on, and publishing an
+// aggregate waits for nothing.
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
                                                          uint32_t total_items, const Scratch s, uint32_t* error,
@@ -124,6 +127,11 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         const ViewJob& J = job[jb];
         const uint32_t n = J.n;
         const uint32_t b = (item - J.first_item) * (uint32_t)T::SIZE;
+        // The next item is taken now; its round trip is hidden behind this
+        // item's loads, arithmetic and scan (its value is first needed
+        // after the scan).
+        uint32_t nxt = 0;
+        if (t == kHandoff) nxt = atomicAdd(&s.ctl->tile_counter, 1u);
         uint32_t vis_bits = 0, lod_bits = 0;
         uint32_t geo[IPT];
         float4 wsv[IPT];
@@ -161,7 +169,6 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         // next item.
         if (t == 0) T::publish(S, s.tile_state, item, J.first_item, off, b, fault);
         if (t == kHandoff) {
-            const uint32_t nxt = atomicAdd(&s.ctl->tile_counter, 1u);
             const uint32_t nj = find_job(jobs, num_jobs, cur_job, nxt);
             sm[cur ^ 1u].info[0] = nxt;
             s_next_job = nj;

@@ -386,6 +386,43 @@ CADR_API cadr_status cadr_download(cadr_context* ctx, void* dst_host, const void
     return CADR_OK;
 }
 
+CADR_API cadr_status cadr_download_commands(cadr_context* ctx, cadr_draw_indexed_cmd* host_cmds,
+                                            const cadr_draw_indexed_cmd* device_cmds, const uint32_t* host_counts,
+                                            const uint32_t* host_offsets, uint32_t num_state_sets, uint64_t* bytes,
+                                            cadr_stream stream)
+{
+    if (!ctx || !host_counts || !host_offsets || (num_state_sets && (!host_cmds || !device_cmds)))
+        return fail(CADR_ERR_INVALID_ARG, "download_commands: null argument");
+    DeviceGuard dg(ctx->device);
+    for (uint32_t k = 0; k < num_state_sets; k++)
+        if (host_offsets[k + 1] < host_offsets[k] || host_counts[k] > host_offsets[k + 1] - host_offsets[k])
+            return fail(CADR_ERR_INVALID_ARG, "download_commands: count %u exceeds StateSet region %u", host_counts[k], k);
+    cudaStream_t st = pick_stream(ctx, stream);
+    uint64_t total = 0;
+    uint32_t k = 0;
+    while (k < num_state_sets) {
+        if (!host_counts[k]) {
+            k++;
+            continue;
+        }
+        // Regions whose valid parts touch (every region before the last one
+        // of the run full) go in one copy.
+        const uint32_t first = host_offsets[k];
+        uint32_t end = first + host_counts[k];
+        while (k + 1 < num_state_sets && end == host_offsets[k + 1] && host_counts[k + 1]) {
+            k++;
+            end = host_offsets[k] + host_counts[k];
+        }
+        const size_t nbytes = (size_t)(end - first) * sizeof(cadr_draw_indexed_cmd);
+        const cudaError_t e = cudaMemcpyAsync(host_cmds + first, device_cmds + first, nbytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_fail(e, "download_commands");
+        total += nbytes;
+        k++;
+    }
+    if (bytes) *bytes = total;
+    return CADR_OK;
+}
+
 CADR_API cadr_status cadr_stream_synchronize(cadr_stream stream)
 {
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));

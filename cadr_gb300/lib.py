@@ -123,6 +123,7 @@ _SIGS = {
     "cadr_upload": ([vp, vp, vp, sz, vp], i32),
     "cadr_download": ([vp, vp, vp, sz, vp], i32),
     "cadr_stream_synchronize": ([vp], i32),
+    "cadr_download_commands": ([vp, vp, vp, vp, vp, u32, C.POINTER(u64), vp], i32),
     "cadr_process_drawables": ([vp, u32, vp, vp, u64, vp, vp, vp], i32),
     "cadr_scene_create": ([vp, C.POINTER(SceneDesc), C.POINTER(vp)], i32),
     "cadr_scene_destroy": ([vp], i32),

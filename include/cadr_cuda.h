@@ -200,6 +200,18 @@ CADR_API cadr_status cadr_upload(cadr_context* ctx, void* dst_device, const void
                                  size_t bytes, cadr_stream stream);
 CADR_API cadr_status cadr_download(cadr_context* ctx, void* dst_host, const void* src_device,
                                    size_t bytes, cadr_stream stream);
+/* Reads the valid commands of a plain pass back to host memory: for every
+ * StateSet s, the host_counts[s] records at host_offsets[s] of device_cmds
+ * go to the same index of host_cmds (host_counts: the pass's counts, read
+ * back first; host_offsets: the S+1 region offsets).  Regions whose valid
+ * parts touch are copied together; *bytes (optional) receives the bytes
+ * copied.  Stream-ordered on `stream`; host_cmds should be pinned.  No
+ * reference counterpart: the reference's draws never leave the device; this
+ * serves a caller that processes the culled draw list on the host. */
+CADR_API cadr_status cadr_download_commands(cadr_context* ctx, cadr_draw_indexed_cmd* host_cmds,
+                                            const cadr_draw_indexed_cmd* device_cmds, const uint32_t* host_counts,
+                                            const uint32_t* host_offsets, uint32_t num_state_sets, uint64_t* bytes,
+                                            cadr_stream stream);
 CADR_API cadr_status cadr_stream_synchronize(cadr_stream stream);
 
 /* ------------------------------------------------------------------------ */

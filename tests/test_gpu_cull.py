@@ -265,6 +265,35 @@ def test_bad_parent_index_is_reported(ctx):
     assert res["counts"].sum() > 0
 
 
+def test_download_commands_reads_the_valid_prefixes(ctx):
+    """cadr_download_commands copies exactly each region's valid commands
+    to the same index of host memory (touching ranges merged), leaves the
+    rest alone, and rejects a count larger than its region."""
+    import ctypes
+    sc = scenes.small_scene(seed=21, n=50_000, num_levels=2, num_state_sets=40, num_lods=3, empty_state_sets=(3, 4))
+    res, ds, out = gpu_cull(ctx, sc)
+    counts = np.ascontiguousarray(res["counts"], np.uint32)
+    offs = np.ascontiguousarray(sc.state_set_offsets, np.uint32)
+    host = lib.PinnedBuffer(sc.n * 20)
+    h = host.view(np.uint8, (sc.n * 20,))
+    h[:] = 0xAB
+    nbytes = ctypes.c_uint64()
+    lib.check(ctx.lib.cadr_download_commands(ctx.handle, host.ptr, out.cmds.ptr, counts.ctypes.data, offs.ctypes.data,
+                                             sc.num_state_sets, ctypes.byref(nbytes), None))
+    ctx.sync()
+    assert nbytes.value == 20 * int(counts.sum())
+    got = host.view(scenes.CMD_DTYPE, (sc.n,))
+    valid = np.zeros(sc.n, bool)
+    for s_ in range(sc.num_state_sets):
+        valid[offs[s_]:offs[s_] + counts[s_]] = True
+    assert np.array_equal(bits(got[valid]), bits(res["cmds"][valid]))
+    assert (h.reshape(sc.n, 20)[~valid] == 0xAB).all()
+    bad = counts.copy()
+    bad[0] = offs[1] - offs[0] + 1
+    assert ctx.lib.cadr_download_commands(ctx.handle, host.ptr, out.cmds.ptr, bad.ctypes.data, offs.ctypes.data,
+                                          sc.num_state_sets, None, None) == lib.INVALID_ARG
+
+
 def test_stream_mix_probe_measures_bandwidth(ctx):
     """cadr_measure_stream_mix (the bench's same-traffic ceiling) runs and
     returns a bandwidth, and rejects an empty size."""
