@@ -64,31 +64,17 @@ __device__ __forceinline__ uint32_t find_job(const ViewJob* __restrict__ jobs, u
     return lo;
 }
 
-// One thread copies a job record into shared memory (16-byte words, all
-// loads in flight together).
-__device__ __forceinline__ void copy_job(const ViewJob* __restrict__ src, ViewJob* dst)
-{
-    static_assert(sizeof(ViewJob) % 16 == 0, "job record in 16-byte words");
-    constexpr int kWords = sizeof(ViewJob) / 16;
-    uint4 w[kWords];
-#pragma unroll
-    for (int k = 0; k < kWords; k++) w[k] = __ldg(reinterpret_cast<const uint4*>(src) + k);
-#pragma unroll
-    for (int k = 0; k < kWords; k++) reinterpret_cast<uint4*>(dst)[k] = w[k];
-}
-
-// The persistent kernel.  Per item: load and classify, barrier, tile scan
-// (barrier inside), publish and look back while the LOD entries are
-// gathered and the next item is taken, barrier, write.  The per-item tile
-// state is double-buffered (item k uses sm[k & 1]), and so are the job
-// record and the staged StateSet offsets (switched when the job changes),
-// so item k+1's ballots and job never overwrite what item k's write phase
-// reads: three CTA barriers per item.  The next item is taken by the first
-// thread of warp 1 (warp 0 does the lookback) when the current one starts,
-// and published with its job by the carry barrier.  A CTA thus holds one
-// item it has not started; every wait still ends, since the smallest
-// unpublished item is always one a CTA is working on, and publishing an
-// aggregate waits for nothing.
+// The persistent kernel.  Per item: thread 0 publishes the item (and its
+// job) by the first barrier; load and classify, barrier; warp 0 scans the
+// tile, publishes the tile's aggregate and looks back while the other
+// warps gather their LOD entries, barrier; write.  The per-item tile state
+// is double-buffered (item k uses sm[k & 1]), so the next item's ballots
+// never overwrite what a slower warp still reads in this item's write
+// phase, and the first barrier of the next item, which every thread
+// reaches only after its writes, guards the job record: three CTA barriers
+// per item.  Thread 0 takes the next item while the current one's commands
+// are written (the atomic's round trip leaves the critical path), so a CTA
+// holds an item it has not started only for one write phase.
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
                                                          uint32_t total_items, const Scratch s, uint32_t* error,
@@ -96,42 +82,41 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
 {
     using T = Tile<THREADS, IPT>;
     __shared__ typename T::Smem sm[2];
-    __shared__ __align__(16) ViewJob job[2];
-    __shared__ uint32_t s_next_job;
-    extern __shared__ uint32_t s_offsets[];  // two areas of kBatchedOffsetCap words
+    __shared__ __align__(16) ViewJob job;
+    __shared__ uint32_t s_item, s_job;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    constexpr int kHandoff = kWarp;
-    if (t == kHandoff) {
-        const uint32_t item = atomicAdd(&s.ctl->tile_counter, 1u);
-        const uint32_t j = find_job(jobs, num_jobs, 0u, item);
-        sm[0].info[0] = item;
-        s_next_job = j;
-        if (item < total_items) copy_job(jobs + j, &job[0]);
-    }
+    extern __shared__ uint32_t s_offsets[];
     if (t == 0) {
         const uint32_t ep = load_relaxed_u32(&s.ctl->epoch);
         sm[0].info[1] = ep;
         sm[1].info[1] = ep;
     }
-    __syncthreads();
-    uint32_t cur = 0, jb = 0, cur_job = s_next_job;
-    // Published by the first item's first barrier.
-    const uint32_t* off = sm[0].info[0] < total_items
-                              ? stage_offsets(s_offsets, kBatchedOffsetCap, job[0].offsets, job[0].num_state_sets)
-                              : nullptr;
+    uint32_t cur = 0, cur_job = 0xffffffffu;
+    const uint32_t* off = nullptr;
+    uint32_t nxt = 0;
+    bool have_next = false;
     for (;;) {
-        typename T::Smem& S = sm[cur];
-        const uint32_t item = S.info[0];
+        if (t == 0) {
+            const uint32_t item = have_next ? nxt : atomicAdd(&s.ctl->tile_counter, 1u);
+            s_item = item;
+            s_job = find_job(jobs, num_jobs, cur_job == 0xffffffffu ? 0u : cur_job, item);
+        }
+        __syncthreads();
+        const uint32_t item = s_item;
         if (item >= total_items) break;
-        const ViewJob& J = job[jb];
-        const uint32_t n = J.n;
-        const uint32_t b = (item - J.first_item) * (uint32_t)T::SIZE;
-        // The next item is taken now; its round trip is hidden behind this
-        // item's loads, arithmetic and scan (its value is first needed
-        // after the scan).
-        uint32_t nxt = 0;
-        if (t == kHandoff) nxt = atomicAdd(&s.ctl->tile_counter, 1u);
+        if (s_job != cur_job) {
+            cur_job = s_job;
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + cur_job);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&job);
+            for (int k = t; k < (int)(sizeof(ViewJob) / 4); k += THREADS) dst[k] = __ldg(src + k);
+            __syncthreads();
+            // published by the __syncthreads() that follows the item loop
+            off = stage_offsets(s_offsets, kBatchedOffsetCap, job.offsets, job.num_state_sets);
+        }
+        typename T::Smem& S = sm[cur];
+        const uint32_t n = job.n;
+        const uint32_t b = (item - job.first_item) * (uint32_t)T::SIZE;
         uint32_t vis_bits = 0, lod_bits = 0;
         uint32_t geo[IPT];
         float4 wsv[IPT];
@@ -140,8 +125,8 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
         for (int j = 0; j < IPT; j++) {
             const uint32_t i = b + (uint32_t)(j * THREADS + t);
             const uint32_t ic = i < n ? i : 0u;
-            wsv[j] = n ? ld_nc_f4(J.world_sphere + ic) : make_float4(0.f, 0.f, 0.f, 0.f);
-            geo[j] = n ? ld_nc_u32(J.geometry + ic) : 0u;
+            wsv[j] = n ? ld_nc_f4(job.world_sphere + ic) : make_float4(0.f, 0.f, 0.f, 0.f);
+            geo[j] = n ? ld_nc_u32(job.geometry + ic) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
@@ -149,7 +134,7 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
             bool visible = false, marginal = false;
             uint32_t lod = 0;
             if (i < n)
-                classify(J.view, wsv[j], J.num_lods, visible, marginal, lod);
+                classify(job.view, wsv[j], job.num_lods, visible, marginal, lod);
             else
                 geo[j] = 0;
             const uint32_t vb = __ballot_sync(~0u, visible);
@@ -157,38 +142,29 @@ __global__ void __launch_bounds__(THREADS) batched_kernel(const ViewJob* __restr
             const uint32_t word0 = b + (uint32_t)(j * THREADS + warp * kWarp);
             if (lane == 0) {
                 S.ballot[j][warp] = vb;
-                if (J.marginal && word0 < n) J.marginal[word0 >> 5] = mb;
+                if (job.marginal && word0 < n) job.marginal[word0 >> 5] = mb;
             }
             vis_bits |= (visible ? 1u : 0u) << j;
             lod_bits |= lod << (2 * j);
         }
         __syncthreads();
-        T::scan(S, off, J.num_state_sets, b, n);
-        // The aggregate goes out first; the LOD entries are gathered while
-        // warp 0 waits for its predecessor's prefix, and warp 1 takes the
-        // next item.
-        if (t == 0) T::publish(S, s.tile_state, item, J.first_item, off, b, fault);
-        if (t == kHandoff) {
-            const uint32_t nj = find_job(jobs, num_jobs, cur_job, nxt);
-            sm[cur ^ 1u].info[0] = nxt;
-            s_next_job = nj;
-            if (nxt < total_items && nj != cur_job) copy_job(jobs + nj, &job[jb ^ 1u]);
+        // Warp 0 scans the tile and publishes its aggregate first; the LOD
+        // entries are gathered while it waits for its predecessor's prefix.
+        if (warp == 0) {
+            T::scan_warp0(S, off, job.num_state_sets, b, n);
+            if (t == 0) T::publish(S, s.tile_state, item, job.first_item, off, b, fault);
         }
         uint4 ent[IPT];
-        T::gather(vis_bits, lod_bits, geo, J.lods, J.num_geometries, J.num_lods, error, ent);
-        if (warp == 0) T::resolve(S, s.tile_state, item, J.first_item, limit_ns, error);
+        T::gather(vis_bits, lod_bits, geo, job.lods, job.num_geometries, job.num_lods, error, ent);
+        if (warp == 0) T::resolve(S, s.tile_state, item, job.first_item, limit_ns, error);
         __syncthreads();
-        T::write_ent(S, vis_bits, ent, b, n, item == J.first_item, off, J.num_state_sets, J.cmds, J.counts, error);
-        const uint32_t nj = s_next_job;
-        cur ^= 1u;
-        if (nj != cur_job && sm[cur].info[0] < total_items) {
-            // The new job's offsets go to the other area; the next item's
-            // first barrier publishes them.
-            cur_job = nj;
-            jb ^= 1u;
-            off = stage_offsets(s_offsets + jb * kBatchedOffsetCap, kBatchedOffsetCap, job[jb].offsets,
-                                job[jb].num_state_sets);
+        if (t == 0) {
+            nxt = atomicAdd(&s.ctl->tile_counter, 1u);
+            have_next = true;
         }
+        T::write_ent(S, vis_bits, ent, b, n, item == job.first_item, off, job.num_state_sets, job.cmds, job.counts,
+                     error);
+        cur ^= 1u;
     }
     if (t == 0) finish_pass(s.ctl);
 }
@@ -229,8 +205,8 @@ cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32
 {
     KernelFn k = pick_kernel(block_threads, items_per_thread);
     if (!k) return cudaErrorInvalidValue;
-    k<<<grid, block_threads, 2 * kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s,
-                                                                              error, spin_limit_ns, fault);
+    k<<<grid, block_threads, kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s, error,
+                                                                          spin_limit_ns, fault);
     return cudaGetLastError();
 }
 

@@ -183,6 +183,15 @@ CADR_API cadr_status cadr_context_create(int device, cadr_context** out)
     auto* ctx = new cadr_context();
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    // The pass's scattered reads are 4 to 16 bytes wide (handle-table
+    // entries, MatrixList headers, parent matrices, LOD entries): DRAM
+    // fetches of 32-byte sectors move the fewest unused bytes.  A hint of
+    // this process's context, given back when the context is destroyed.
+    if (cudaDeviceGetLimit(&ctx->prev_l2_fetch, cudaLimitMaxL2FetchGranularity) == cudaSuccess &&
+        cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, kL2FetchBytes) == cudaSuccess)
+        ctx->l2_fetch_set = true;
+    else
+        cudaGetLastError();
     e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->upload_done, cudaEventDisableTiming);
@@ -214,6 +223,7 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
     DeviceGuard dg(ctx->device);
     cudaDeviceSynchronize();
     destroy_batched_state(ctx);
+    if (ctx->l2_fetch_set) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, ctx->prev_l2_fetch);
     scratch_release(ctx->scratch);
     scratch_release(ctx->shard_scratch);
     for (int f = 0; f < cadr_context::kFrames; f++) {

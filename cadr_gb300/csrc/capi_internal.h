@@ -13,6 +13,8 @@
 
 namespace cadr {
 constexpr int kRingSlots = 2;
+// L2 fetch granularity the context sets for the process (bytes).
+constexpr size_t kL2FetchBytes = 32;
 struct BatchedState;
 }
 
@@ -29,6 +31,8 @@ struct cadr_context {
     size_t ring_bytes = size_t(64) << 20;
     int ring_next = 0;
     std::mutex ring_mu;
+    size_t prev_l2_fetch = 0;              // the device's L2 fetch granularity before this context
+    bool l2_fetch_set = false;
     uint32_t* h_error = nullptr;           // mapped pinned error word
     uint32_t* d_error = nullptr;
     uint64_t spin_limit_ns = 1000000000ull;

@@ -132,6 +132,49 @@ struct Tile {
         __syncthreads();
     }
 
+    // Warp 0 alone, after the ballots are stored and a __syncthreads(): the
+    // same results as scan() (ballot-count prefix, total, the regions of
+    // the tile's first and last drawable, lanes 0 and 1 searching at once),
+    // with no CTA barrier; warp 0 sees them after its own __syncwarp(), the
+    // other warps after the caller's next __syncthreads().
+    __device__ static __forceinline__ void scan_warp0(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
+                                                      uint32_t b, uint32_t n)
+    {
+        const int lane = threadIdx.x & 31;
+        constexpr int PER = (NC + 31) / 32;
+        uint32_t c[PER];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const int idx = lane * PER + k;
+            c[k] = idx < NC ? __popc(sm.ballot[idx / NW][idx % NW]) : 0u;
+            sum += c[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(~0u, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const int idx = lane * PER + k;
+            if (idx < NC) sm.prefix[idx] = run;
+            run += c[k];
+        }
+        if (lane == 31) sm.info[3] = incl;
+        if (lane < 2) {
+            // Clamped to S-1 so that an empty scene (n == 0, one work item)
+            // stays inside the offsets and counts arrays.
+            const uint32_t e = min(b + (uint32_t)SIZE, n);
+            const uint32_t key = lane == 0 ? b : (n ? e - 1 : 0u);
+            const uint32_t r = (lane == 1 && !n) ? S - 1 : min(region_of(offsets, 0, S + 1, key), S - 1);
+            sm.info[4 + lane] = r;
+        }
+        __syncwarp();
+    }
+
     // One lane of warp 0, after scan(): publish the tile's aggregate (the
     // scan's first item publishes its inclusive prefix at once) and keep the
     // published value and head flag in info[6], info[7] for resolve().

@@ -454,18 +454,18 @@ __global__ void __launch_bounds__(kPropThreads) propagate_kernel(
     st_f8(wp + 2, mat_col(p0, p1, p2, p3, l2), mat_col(p0, p1, p2, p3, l3));
 }
 
-constexpr int kFoldThreads = 1024;
+constexpr int kFoldThreads = 256;
 
 __host__ __device__ constexpr uint32_t pad16_words(uint32_t n) { return (n + 3u) & ~3u; }
 
-// Shared memory of the folded levels at their maximum: 64 B per node (level
-// 0 and every folded level), the parent indices of the folded levels
-// (each level padded to 16 bytes).
-constexpr size_t kFoldSmemBytes = kFoldMaxNodes * 64 + (kFoldMaxNodes + 4 * CADR_MAX_LEVELS) * 4;
+// Shared memory of the folded levels: 64 B per node (level 0 and every
+// folded level), then the parent indices of the folded levels (each level
+// padded to 16 bytes).
+constexpr size_t kFoldSmemWords = kFoldMaxNodes * 16 + kFoldMaxNodes + 4 * CADR_MAX_LEVELS;
 
 __global__ void __launch_bounds__(kFoldThreads) propagate_small_levels_kernel(const FoldArgs a)
 {
-    extern __shared__ __align__(128) float4 s_mat[];  // level 0, then each folded level: 4 float4 per node
+    __shared__ __align__(128) float4 s_mat[kFoldSmemWords / 4];  // level 0, then each folded level: 4 float4 per node
     __shared__ __align__(8) uint64_t s_bar;
     // The next level kernel (or the stream kernel) may launch now: it reads
     // these levels' world matrices only after griddepcontrol.wait.
@@ -533,21 +533,10 @@ __global__ void __launch_bounds__(kFoldThreads) propagate_small_levels_kernel(co
 
 cudaError_t launch_small_levels(const FoldArgs& a, cudaStream_t stream)
 {
-    static bool attr_set = false;
-    if (!attr_set) {
-        const cudaError_t e = cudaFuncSetAttribute(propagate_small_levels_kernel,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFoldSmemBytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    uint32_t total = a.n0, par_words = 0;
-    for (uint32_t l = 0; l < a.count; l++) {
-        total += a.lvl[l].n;
-        par_words += pad16_words(a.lvl[l].n);
-    }
-    if (total > kFoldMaxNodes) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)total * 64 + (size_t)par_words * 4;
-    propagate_small_levels_kernel<<<1, kFoldThreads, smem, stream>>>(a);
+    uint32_t total = a.n0;
+    for (uint32_t l = 0; l < a.count; l++) total += a.lvl[l].n;
+    if (total > kFoldMaxNodes || a.count == 0 || a.count >= CADR_MAX_LEVELS) return cudaErrorInvalidValue;
+    propagate_small_levels_kernel<<<1, kFoldThreads, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -167,7 +167,10 @@ CADR_API int cadr_abi_version(void);
 
 /* Creates the per-device context: streams (compute + upload), pinned staging
  * ring and lookback scratch.  Replaces the Vulkan device/queue the reference
- * Renderer is constructed with (src/CadR/Renderer.h:124-128). */
+ * Renderer is constructed with (src/CadR/Renderer.h:124-128).  It sets the
+ * process's L2 fetch granularity hint on the device to 32 bytes (the pass's
+ * scattered reads are 4-16 bytes wide) and gives the previous value back in
+ * cadr_context_destroy. */
 CADR_API cadr_status cadr_context_create(int device, cadr_context** out);
 CADR_API cadr_status cadr_context_destroy(cadr_context* ctx);
 CADR_API cadr_stream cadr_context_stream(cadr_context* ctx);

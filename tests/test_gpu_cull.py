@@ -126,20 +126,20 @@ def test_c3_full_size_against_oracle(ctx):
     res["world"] = ctx.download(ds.buffers().world, np.float32, (sc.n, 16))
     ref = bind.cull(sc, sc.views[0], threads=bind.max_threads(), want_world=True)
     assert_same(res, ref, sc.state_set_offsets)
-    # Levels 1-4 (2 + 24 + 216 + 1,982 nodes, with level 0's one node under
-    # the 3,072 of one CTA's shared memory) run folded in one launch, whose
-    # time frame timing gives to level 1.
+    # Levels 1-3 (2 + 24 + 216 nodes, with level 0's one node within the
+    # 256 of the folded launch) run in one launch, whose time frame timing
+    # gives to level 1.
     lv = frames[0][4]
     assert len(frames) == 1 and len(lv) == 7
-    assert lv[0] > 0 and all(t >= 0 for t in lv) and all(t > 0 for t in lv[4:])
+    assert lv[0] > 0 and all(t >= 0 for t in lv) and all(t > 0 for t in lv[3:])
     assert sum(lv) <= frames[0][0] * 1.01 + 1e-3
     assert ctx.launch_count > 0
 
 
 @pytest.mark.parametrize("n,levels,fanout", [
-    (40_000, 6, 4),    # levels 1-3 folded (with level 0: 9 + 39 + 156 + 625 nodes), 4-5 launched one by one
-    (3_000, 5, 3),     # every internal level folded
-    (200_000, 8, 3),   # folded, then four level kernels
+    (40_000, 6, 4),    # levels 1-2 folded (with level 0: 9 + 39 + 156 nodes), 3-5 launched one by one
+    (400, 4, 3),       # every internal level folded (14 + 44 + 133 nodes)
+    (200_000, 8, 4),   # levels 1-2 folded (3 + 12 + 48 nodes), then five level kernels
 ])
 def test_folded_levels_against_oracle(ctx, n, levels, fanout):
     sc = scenes.small_scene(seed=n + levels, n=n, num_levels=levels, num_state_sets=7, num_lods=3, fanout=fanout)
