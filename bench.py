@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--plain-duration", type=float, default=10.0,
                     help="serving: seconds of the request stream the one-request-per-launch loop serves")
     ap.add_argument("--form", default="plain", choices=["plain", "serving", "tier-a", "batched", "c3"])
-    ap.add_argument("--batched-tuning", default="", help="batched: block_threads,items_per_thread,ctas_per_sm "
+    ap.add_argument("--batched-tuning", default="", help="batched: block_threads,items_per_thread,ctas_per_sm[,form] "
                                                            "instead of the autotuner's pick")
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of request stream")
@@ -310,8 +310,8 @@ def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_overr
             plain_outs.append(lib.CullOutputs(ctx, sc.n, sc.num_state_sets, marginal=False))
     arr = lib.batch_views(items)
     if tuning_override:
-        bt, ipt, cps = (int(x) for x in tuning_override.split(","))
-        ctx.set_tuning(bt, ipt, cps)
+        f = [int(x) for x in tuning_override.split(",")]
+        ctx.set_tuning(f[0], f[1], f[2], f[3] if len(f) > 3 else 0)
         tuning, tune_ms = ctx.get_tuning(), None
     else:
         tuning, tune_ms = lib.autotune_batched(ctx, arr, reps=3)
@@ -376,7 +376,9 @@ def run_batched(ctx, steps: int, warmup: int, num_scenes: int = 32, tuning_overr
         "plain_gitems_per_s": view_items / (res["plain"][0] / 1e3) / 1e9,
         "launches_per_step": {"plain": res["plain"][1], "batched": res["batched"][1]},
         "tuning": {"block_threads": tuning.block_threads, "items_per_thread": tuning.items_per_thread,
-                   "ctas_per_sm": tuning.ctas_per_sm, "autotune_ms": tune_ms},
+                   "ctas_per_sm": tuning.ctas_per_sm,
+                   "form": "three-launch" if tuning.form == lib.BATCHED_THREE_LAUNCH else "persistent",
+                   "autotune_ms": tune_ms},
         "bit_identical": identical,
         "roofline": {"bound": "issue", "algorithmic_bytes": batched_bytes, "achieved_gbs": gbs,
                      "frac_of_hbm": gbs / peak, "thread_instructions_per_item": ipi,

@@ -173,6 +173,152 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batched_kernel(const 
     if (t == 0) finish_pass(s.ctl);
 }
 
+// ---------------------------------------------------------------------------
+// The three-launch form (tuning form 1): classify, per-view tile scan,
+// write, over the same view-major (view, tile) items with tiles of
+// kLeafTile drawables, so that each scene's per-tile region-start table
+// serves it.  No CTA waits for another: a reduce-then-scan like the plain
+// pass, with every view's first tile a scan head.
+
+// The job of work item `item`, found by one warp: each round its lanes
+// probe 32 evenly spaced jobs and keep the last whose first item is at or
+// below `item` (two rounds up to 1,024 jobs).  jobs[0].first_item is 0.
+__device__ __forceinline__ uint32_t warp_find_job(const ViewJob* __restrict__ jobs, uint32_t num_jobs, uint32_t item)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo = 0, hi = num_jobs;  // the job is in [lo, hi); jobs[lo].first_item <= item
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31u) / 32u;
+        const uint32_t k = lo + lane * step;
+        const uint32_t m = __ballot_sync(~0u, k < hi && __ldg(&jobs[k].first_item) <= item);
+        lo += (31u - (uint32_t)__clz(m)) * step;  // lane 0 always holds: bit 0 is set
+        hi = min(hi, lo + step);
+    }
+    return lo;
+}
+
+// Words of one bit-plane of a batch: 64 per item (2,048 drawables), padded
+// to 16 bytes.  Three planes (visibility, LOD bits 0 and 1), then one tile
+// word per item.
+__host__ __device__ constexpr uint64_t batched_plane_stride(uint64_t items) { return (items * 64 + 3) & ~uint64_t(3); }
+
+// Launch 1: one CTA per item classifies its drawables into the planes and
+// writes the item's tile word (as the plain pass's stream kernel does from
+// its matrices, here from the scene's world spheres).
+__global__ void __launch_bounds__(kLeafThreads) batched_classify_kernel(const ViewJob* __restrict__ jobs,
+                                                                       uint32_t num_jobs, uint32_t* __restrict__ planes,
+                                                                       uint64_t stride)
+{
+    __shared__ ViewConst s_view;
+    __shared__ uint32_t ballot[kLeafIpt][kLeafWarps];
+    __shared__ uint32_t s_last_start;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t item = blockIdx.x;
+    const ViewJob* J = jobs + warp_find_job(jobs, num_jobs, item);
+    const uint32_t n = J->n, num_lods = J->num_lods;
+    const uint32_t tile = item - J->first_item;
+    const uint32_t b = tile * (uint32_t)kLeafTile;
+    if (warp == 0) {
+        if (lane < (int)(sizeof(ViewConst) / 16))
+            reinterpret_cast<uint4*>(&s_view)[lane] = __ldg(reinterpret_cast<const uint4*>(&J->view) + lane);
+        if (lane == 31) s_last_start = n ? __ldg(J->tile_start + tile) : 0u;
+    }
+    const float4* ws = J->world_sphere;
+    uint32_t* marginal = J->marginal;
+    float4 wsv[kLeafIpt];
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        const uint32_t i = b + (uint32_t)(j * kLeafThreads + t);
+        wsv[j] = i < n ? ld_nc_f4(ws + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const uint64_t base = (uint64_t)item * 64;
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
+        bool visible = false, mar = false;
+        uint32_t lod = 0;
+        if (i0 + (uint32_t)lane < n) classify(s_view, wsv[j], num_lods, visible, mar, lod);
+        const uint32_t vb = __ballot_sync(~0u, visible);
+        const uint32_t mb = __ballot_sync(~0u, mar);
+        const uint32_t lb0 = __ballot_sync(~0u, (lod & 1u) != 0u);
+        const uint32_t lb1 = __ballot_sync(~0u, (lod & 2u) != 0u);
+        if (lane == 0) {
+            ballot[j][warp] = vb;
+            if (i0 < n) {
+                const uint64_t w = base + (uint64_t)(j * kLeafWarps + warp);
+                planes[w] = vb;
+                planes[stride + w] = lb0;
+                planes[2 * stride + w] = lb1;
+                if (marginal) marginal[i0 >> 5] = mb;
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = leaf_tile_word(ballot, s_last_start, b);
+        if (lane == 0) planes[3 * stride + item] = w;
+    }
+}
+
+// Launch 2: one CTA per view turns its items' tile words into carries.
+constexpr int kBatchedScanThreads = 256;
+__global__ void __launch_bounds__(kBatchedScanThreads) batched_tile_scan_kernel(const ViewJob* __restrict__ jobs,
+                                                                               uint32_t* __restrict__ words)
+{
+    grid_dependents_launch();
+    const ViewJob* J = jobs + blockIdx.x;
+    const uint32_t lo = J->first_item;
+    scan_tile_words<kBatchedScanThreads, 4>(words, lo, lo + J->num_tiles);
+}
+
+// Launch 3: one CTA per item writes its commands and counts, as the plain
+// pass's write kernel does; a programmatic dependent of the scan, it reads
+// only the carry after griddepcontrol.wait (the planes come from launch 1,
+// complete before the scan started).
+__global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) batched_write_kernel(const ViewJob* __restrict__ jobs,
+                                                                                     uint32_t num_jobs,
+                                                                                     const uint32_t* __restrict__ planes,
+                                                                                     uint64_t stride, uint32_t* error)
+{
+    __shared__ LeafTile::Smem sm;
+    extern __shared__ uint32_t s_off[];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t item = blockIdx.x;
+    const ViewJob* J = jobs + warp_find_job(jobs, num_jobs, item);
+    const uint32_t n = J->n, S = J->num_state_sets;
+    const uint32_t tile = item - J->first_item;
+    const uint32_t b = tile * (uint32_t)kLeafTile;
+    const uint32_t* off = stage_offsets(s_off, kWriteOffsetCap, J->offsets, S);
+    const uint32_t* geometry = J->geometry;
+    const uint64_t base = (uint64_t)item * 64;
+    uint32_t vw[kLeafIpt], l0[kLeafIpt], l1[kLeafIpt], geo[kLeafIpt];
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
+        const uint32_t i = i0 + (uint32_t)lane;
+        const uint64_t w = base + (uint64_t)(j * kLeafWarps + warp);
+        vw[j] = i0 < n ? __ldg(planes + w) : 0u;
+        l0[j] = i0 < n ? __ldg(planes + stride + w) : 0u;
+        l1[j] = i0 < n ? __ldg(planes + 2 * stride + w) : 0u;
+        geo[j] = i < n ? __ldg(geometry + i) : 0u;
+    }
+    uint32_t vis_bits = 0, lod_bits = 0;
+#pragma unroll
+    for (int j = 0; j < kLeafIpt; j++) {
+        vis_bits |= ((vw[j] >> lane) & 1u) << j;
+        lod_bits |= (((l0[j] >> lane) & 1u) | (((l1[j] >> lane) & 1u) << 1)) << (2 * j);
+        if (lane == 0) sm.ballot[j][warp] = vw[j];
+    }
+    uint4 ent[kLeafIpt];
+    LeafTile::gather(vis_bits, lod_bits, geo, J->lods, J->num_geometries, J->num_lods, error, ent);
+    grid_dependency_wait();
+    if (t == 0) sm.info[2] = load_relaxed_u32(planes + 3 * stride + item);
+    __syncthreads();
+    LeafTile::scan(sm, off, S, b, n);
+    LeafTile::write_ent(sm, vis_bits, ent, b, n, tile == 0, off, S, J->cmds, J->counts, error);
+}
+
 using KernelFn = void (*)(const ViewJob*, uint32_t, uint32_t, const Scratch, uint32_t*, uint64_t, uint32_t);
 
 template <int TH>
@@ -198,19 +344,44 @@ KernelFn pick_kernel(uint32_t threads, uint32_t ipt)
 
 }  // namespace
 
-uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread)
+uint32_t batched_tile(const cadr_tuning& tu)
 {
-    return block_threads * items_per_thread;
+    return tu.form == kBatchedThreeLaunch ? (uint32_t)kLeafTile : tu.block_threads * tu.items_per_thread;
+}
+
+uint64_t batched_plane_words(const cadr_tuning& tu, uint64_t total_items)
+{
+    return tu.form == kBatchedThreeLaunch ? 3 * batched_plane_stride(total_items) + ((total_items + 3) & ~uint64_t(3))
+                                          : 0;
 }
 
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items, Scratch& s,
-                                uint32_t* error, uint64_t spin_limit_ns, uint32_t fault, uint32_t block_threads,
-                                uint32_t items_per_thread, uint32_t grid, cudaStream_t stream)
+                                uint32_t* error, uint64_t spin_limit_ns, uint32_t fault, const cadr_tuning& tu,
+                                uint32_t grid, cudaStream_t stream)
 {
-    KernelFn k = pick_kernel(block_threads, items_per_thread);
+    if (tu.form == kBatchedThreeLaunch) {
+        if (total_items == 0) return cudaSuccess;
+        const uint64_t stride = batched_plane_stride(total_items);
+        batched_classify_kernel<<<total_items, kLeafThreads, 0, stream>>>(d_jobs, num_jobs, s.planes, stride);
+        batched_tile_scan_kernel<<<num_jobs, kBatchedScanThreads, 0, stream>>>(d_jobs, s.planes + 3 * stride);
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr.val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(total_items);
+        cfg.blockDim = dim3(kLeafThreads);
+        cfg.dynamicSmemBytes = kWriteOffsetCap * sizeof(uint32_t);
+        cfg.stream = stream;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, batched_write_kernel, d_jobs, num_jobs,
+                                                 (const uint32_t*)s.planes, stride, error);
+        return e == cudaSuccess ? cudaGetLastError() : e;
+    }
+    KernelFn k = pick_kernel(tu.block_threads, tu.items_per_thread);
     if (!k) return cudaErrorInvalidValue;
-    k<<<grid, block_threads, kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s, error,
-                                                                          spin_limit_ns, fault);
+    k<<<grid, tu.block_threads, kBatchedOffsetCap * sizeof(uint32_t), stream>>>(d_jobs, num_jobs, total_items, s,
+                                                                             error, spin_limit_ns, fault);
     return cudaGetLastError();
 }
 
@@ -230,7 +401,9 @@ void destroy_batched_state(cadr_context* ctx)
 
 bool tuning_valid(const cadr_tuning& t)
 {
-    return pick_kernel(t.block_threads, t.items_per_thread) != nullptr && t.ctas_per_sm >= 1 && t.ctas_per_sm <= 16;
+    if (t.ctas_per_sm < 1 || t.ctas_per_sm > 16) return false;
+    if (t.form == kBatchedThreeLaunch) return t.block_threads == (uint32_t)kLeafThreads && t.items_per_thread == (uint32_t)kLeafIpt;
+    return t.form == kBatchedPersistent && pick_kernel(t.block_threads, t.items_per_thread) != nullptr;
 }
 
 // Fills `jobs` for a batch and returns the total number of work items.
@@ -253,6 +426,7 @@ cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, 
         j.cmds = reinterpret_cast<uint32_t*>(bv.cmds);
         j.counts = bv.counts;
         j.marginal = bv.marginal;
+        j.tile_start = sc->tile_start;
         j.n = (uint32_t)sc->desc.num_drawables;
         j.num_state_sets = sc->desc.num_state_sets;
         j.num_geometries = sc->desc.num_geometries;
@@ -285,8 +459,8 @@ CADR_API cadr_status cadr_set_tuning(cadr_context* ctx, const cadr_tuning* t)
 {
     if (!ctx || !t) return fail(CADR_ERR_INVALID_ARG, "set_tuning: null argument");
     if (!tuning_valid(*t))
-        return fail(CADR_ERR_INVALID_ARG, "set_tuning: unsupported block %u / items %u / ctas %u", t->block_threads,
-                    t->items_per_thread, t->ctas_per_sm);
+        return fail(CADR_ERR_INVALID_ARG, "set_tuning: unsupported block %u / items %u / ctas %u / form %u",
+                    t->block_threads, t->items_per_thread, t->ctas_per_sm, t->form);
     ctx->tuning = *t;
     return CADR_OK;
 }
@@ -334,9 +508,10 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
         if (st != CADR_OK) return st;
     }
     uint64_t total = 0;
-    cadr_status st = build_jobs(views, num_views, batched_tile(tu.block_threads, tu.items_per_thread), B.h_jobs, &total);
+    cadr_status st = build_jobs(views, num_views, batched_tile(tu), B.h_jobs, &total);
     if (st != CADR_OK) return st;
     st = scratch_reserve(ctx, B.scratch, total);
+    if (st == CADR_OK) st = scratch_reserve_planes(ctx, B.scratch, batched_plane_words(tu, total));
     if (st != CADR_OK) return st;
     const uint32_t grid = (uint32_t)std::min<uint64_t>(total, (uint64_t)tu.ctas_per_sm * ctx->num_sms);
     const size_t job_bytes = num_views * sizeof(ViewJob);
@@ -354,7 +529,7 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
             if (e != cudaSuccess) return cuda_fail(e, "cull_batched: begin capture");
             cudaError_t e1 = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
             cudaError_t e2 = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error,
-                                                 ctx->spin_limit_ns, ctx->fault, tu.block_threads, tu.items_per_thread, grid, s);
+                                                 ctx->spin_limit_ns, ctx->fault, tu, grid, s);
             e = cudaStreamEndCapture(s, &B.graph);
             if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess) {
                 if (B.graph) cudaGraphDestroy(B.graph);
@@ -377,10 +552,10 @@ CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view*
         e = cudaMemcpyAsync(B.d_jobs, B.h_jobs, job_bytes, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) return cuda_fail(e, "cull_batched: job copy");
         e = launch_batched_cull(B.d_jobs, num_views, (uint32_t)total, B.scratch, ctx->d_error, ctx->spin_limit_ns,
-                                ctx->fault, tu.block_threads, tu.items_per_thread, grid, s);
+                                ctx->fault, tu, grid, s);
         if (e != cudaSuccess) return cuda_fail(e, "cull_batched: launch");
     }
-    ctx->launches++;
+    ctx->launches += tu.form == kBatchedThreeLaunch ? 3 : 1;
     B.scratch.launches++;
     for (uint32_t v = 0; v < num_views; v++) {
         cadr_status st = scene_mark_read(views[v].scene, s);

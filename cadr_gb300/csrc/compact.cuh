@@ -310,6 +310,124 @@ struct Tile {
     }
 };
 
+using LeafTile = Tile<kLeafThreads, kLeafIpt>;
+
+// The tile word of a reduce-then-scan pass: the visible drawables of the
+// tile's last StateSet region that lie in the tile (all of the tile's
+// visible drawables when no region starts in it), and in bit 31 whether a
+// region starts in the tile.
+constexpr uint32_t kTileHead = 0x80000000u;
+
+// Warp 0 (all lanes return it): the tile word of the tile of drawables
+// [b, b + kLeafTile) from its ballots (ballot[j][w] covers the tile's
+// drawables [32 (j kLeafWarps + w), + 32)) and the start of the region
+// holding its last drawable.
+__device__ __forceinline__ uint32_t leaf_tile_word(const uint32_t (*ballot)[kLeafWarps], uint32_t last_start,
+                                                   uint32_t b)
+{
+    const int lane = threadIdx.x & 31;
+    const bool head = last_start >= b;
+    const uint32_t q = head ? last_start - b : 0u;
+    uint32_t total = 0, before = 0;
+#pragma unroll
+    for (int h = 0; h < (kLeafIpt * kLeafWarps) / kWarp; h++) {
+        const uint32_t k = (uint32_t)(lane + h * kWarp);
+        const uint32_t v = ballot[k / kLeafWarps][k % kLeafWarps];
+        total += __popc(v);
+        if (32u * k + 32u <= q)
+            before += __popc(v);
+        else if (32u * k < q)
+            before += __popc(v & ((1u << (q - 32u * k)) - 1u));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        total += __shfl_xor_sync(~0u, total, o);
+        before += __shfl_xor_sync(~0u, before, o);
+    }
+    return head ? (total - before) | kTileHead : total;
+}
+
+// One CTA of THREADS threads replaces the tile words [lo, hi) by their
+// carries: the visible drawables of the region holding the tile's first
+// drawable that precede the tile.  A segmented exclusive scan in chunks of
+// THREADS * PER tiles; a region start in a tile restarts the sum at that
+// tile's count, and the first tile's carry is 0.
+template <int THREADS, int PER>
+__device__ __forceinline__ void scan_tile_words(uint32_t* __restrict__ words, uint32_t lo, uint32_t hi)
+{
+    __shared__ uint32_t s_val[THREADS / kWarp], s_head[THREADS / kWarp];
+    __shared__ uint32_t s_run;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) s_run = 0;
+    __syncthreads();
+    for (uint32_t c0 = lo; c0 < hi; c0 += (uint32_t)(THREADS * PER)) {
+        uint32_t w[PER];
+        uint32_t v = 0, h = 0;  // this thread's segmented total and whether it holds a head
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const uint32_t idx = c0 + (uint32_t)(t * PER + k);
+            w[k] = idx < hi ? words[idx] : 0u;
+            if (w[k] & kTileHead) {
+                v = w[k] & ~kTileHead;
+                h = 1;
+            } else {
+                v += w[k];
+            }
+        }
+        // Inclusive warp scan of (head, value) pairs: a later head resets.
+        uint32_t iv = v, ih = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t pv = __shfl_up_sync(~0u, iv, o), ph = __shfl_up_sync(~0u, ih, o);
+            if (lane >= o && !ih) {
+                iv += pv;
+                ih = ph;
+            }
+        }
+        if (lane == 31) {
+            s_val[warp] = iv;
+            s_head[warp] = ih;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t wv = lane < THREADS / kWarp ? s_val[lane] : 0u, wh = lane < THREADS / kWarp ? s_head[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t pv = __shfl_up_sync(~0u, wv, o), ph = __shfl_up_sync(~0u, wh, o);
+                if (lane >= o && !wh) {
+                    wv += pv;
+                    wh = ph;
+                }
+            }
+            if (lane < THREADS / kWarp) {
+                s_val[lane] = wv;  // inclusive over warps 0..lane
+                s_head[lane] = wh;
+            }
+        }
+        __syncthreads();
+        // Exclusive prefix of this thread: chunk carry-in, earlier warps, earlier lanes.
+        uint32_t ev = s_run;
+        if (warp > 0) {
+            const uint32_t pv = s_val[warp - 1], ph = s_head[warp - 1];
+            ev = ph ? pv : ev + pv;
+        }
+        {
+            const uint32_t pv = __shfl_up_sync(~0u, iv, 1), ph = __shfl_up_sync(~0u, ih, 1);
+            if (lane > 0) ev = ph ? pv : ev + pv;
+        }
+        uint32_t run = ev;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const uint32_t idx = c0 + (uint32_t)(t * PER + k);
+            if (idx < hi) words[idx] = run;
+            run = (w[k] & kTileHead) ? (w[k] & ~kTileHead) : run + w[k];
+        }
+        __syncthreads();
+        if (t == THREADS - 1) s_run = run;
+        __syncthreads();
+    }
+}
+
 // Called by thread 0 of every CTA as its last action: the last CTA of the
 // launch re-arms the control block for the next pass.
 __device__ __forceinline__ void finish_pass(LookbackCtl* ctl)

@@ -29,9 +29,6 @@ __device__ __forceinline__ void load_mat(const float4* __restrict__ p, float4& c
     ld_nc_f8(p + 2, c2, c3);
 }
 
-using LeafTile = Tile<kLeafThreads, kLeafIpt>;
-
-constexpr int kLeafWarps = kLeafThreads / kWarp;
 
 // World matrix records leave through a 2 KB staging block per warp, so
 // that each store instruction of a warp writes 512 contiguous bytes:
@@ -147,12 +144,6 @@ __global__ void __launch_bounds__(kLeafThreads, 4) leaf_propagate_kernel(const L
     stream_tile<false>(a, blockIdx.x * (uint32_t)kLeafTile, nullptr, xb[threadIdx.x >> 5]);
 }
 
-// The tile word of the plain pass's segmented scan: the visible drawables
-// of the tile's last StateSet region that lie in the tile (all of the
-// tile's visible drawables when no region starts in it), and in bit 31
-// whether a region starts in the tile.
-constexpr uint32_t kTileHead = 0x80000000u;
-
 // Plain pass, launch 1 of 3: one CTA per tile streams its drawables
 // (world matrices, world spheres, classification into the planes) and
 // writes the tile word.  No CTA waits for another.
@@ -169,121 +160,25 @@ __global__ void __launch_bounds__(kLeafThreads, 4) leaf_stream_kernel(const Leaf
     stream_tile<true>(a, b, ballot, xb[warp]);
     __syncthreads();
     if (warp == 0) {
-        // Ballot k covers the tile's drawables [32k, 32k + 32).
-        const uint32_t ls = s_last_start;
-        const bool head = ls >= b;
-        const uint32_t q = head ? ls - b : 0u;
-        uint32_t total = 0, before = 0;
-#pragma unroll
-        for (int h = 0; h < (kLeafIpt * kLeafWarps) / kWarp; h++) {
-            const uint32_t k = (uint32_t)(lane + h * kWarp);
-            const uint32_t v = ballot[k / kLeafWarps][k % kLeafWarps];
-            total += __popc(v);
-            if (32u * k + 32u <= q)
-                before += __popc(v);
-            else if (32u * k < q)
-                before += __popc(v & ((1u << (q - 32u * k)) - 1u));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            total += __shfl_xor_sync(~0u, total, o);
-            before += __shfl_xor_sync(~0u, before, o);
-        }
-        if (lane == 0) a.tile_words[tile] = head ? (total - before) | kTileHead : total;
+        const uint32_t w = leaf_tile_word(ballot, s_last_start, b);
+        if (lane == 0) a.tile_words[tile] = w;
     }
 }
 
 // Plain pass, launch 2 of 3, one CTA: replaces every tile word by the
-// tile's carry, the visible drawables of the region holding the tile's
-// first drawable that precede the tile.  A segmented exclusive scan in
-// chunks of 8 tiles per thread; a region start in a tile restarts the sum
-// at that tile's count.  It lets its dependent (the write kernel) launch
-// at once: that kernel reads the carries only after griddepcontrol.wait,
-// which returns when this grid has completed and its writes are visible.
+// tile's carry (scan_tile_words).  It lets its dependent (the write kernel)
+// launch at once: that kernel reads the carries only after
+// griddepcontrol.wait, which returns when this grid has completed and its
+// writes are visible.
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 8;
 
 __global__ void __launch_bounds__(kScanThreads) leaf_tile_scan_kernel(uint32_t* __restrict__ words, uint32_t tiles)
 {
-    __shared__ uint32_t s_val[kScanThreads / kWarp], s_head[kScanThreads / kWarp];
-    __shared__ uint32_t s_run;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     grid_dependents_launch();
-    if (t == 0) s_run = 0;
-    __syncthreads();
-    for (uint32_t c0 = 0; c0 < tiles; c0 += (uint32_t)(kScanThreads * kScanPer)) {
-        uint32_t w[kScanPer];
-        uint32_t v = 0, h = 0;  // this thread's segmented total and whether it holds a head
-#pragma unroll
-        for (int k = 0; k < kScanPer; k++) {
-            const uint32_t idx = c0 + (uint32_t)(t * kScanPer + k);
-            w[k] = idx < tiles ? words[idx] : 0u;
-            if (w[k] & kTileHead) {
-                v = w[k] & ~kTileHead;
-                h = 1;
-            } else {
-                v += w[k];
-            }
-        }
-        // Inclusive warp scan of (head, value) pairs: a later head resets.
-        uint32_t iv = v, ih = h;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t pv = __shfl_up_sync(~0u, iv, o), ph = __shfl_up_sync(~0u, ih, o);
-            if (lane >= o && !ih) {
-                iv += pv;
-                ih = ph;
-            }
-        }
-        if (lane == 31) {
-            s_val[warp] = iv;
-            s_head[warp] = ih;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t wv = s_val[lane], wh = s_head[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t pv = __shfl_up_sync(~0u, wv, o), ph = __shfl_up_sync(~0u, wh, o);
-                if (lane >= o && !wh) {
-                    wv += pv;
-                    wh = ph;
-                }
-            }
-            s_val[lane] = wv;  // inclusive over warps 0..lane
-            s_head[lane] = wh;
-        }
-        __syncthreads();
-        // Exclusive prefix of this thread: chunk carry-in, earlier warps, earlier lanes.
-        uint32_t ev = s_run, eh = 0;
-        if (warp > 0) {
-            const uint32_t pv = s_val[warp - 1], ph = s_head[warp - 1];
-            ev = ph ? pv : ev + pv;
-            eh = ph;
-        }
-        {
-            const uint32_t pv = __shfl_up_sync(~0u, iv, 1), ph = __shfl_up_sync(~0u, ih, 1);
-            if (lane > 0) {
-                ev = ph ? pv : ev + pv;
-                eh |= ph;
-            }
-        }
-        (void)eh;
-        uint32_t run = ev;
-#pragma unroll
-        for (int k = 0; k < kScanPer; k++) {
-            const uint32_t idx = c0 + (uint32_t)(t * kScanPer + k);
-            if (idx < tiles) words[idx] = run;
-            run = (w[k] & kTileHead) ? (w[k] & ~kTileHead) : run + w[k];
-        }
-        __syncthreads();
-        if (t == kScanThreads - 1) s_run = run;
-        __syncthreads();
-    }
+    scan_tile_words<kScanThreads, kScanPer>(words, 0u, tiles);
 }
 
-constexpr uint32_t kWriteOffsetCap = 4096;  // StateSet offsets staged in shared memory
-constexpr int kWriteCtasPerSm = 6;  // 40 registers; 5 and 8 measured slower
 
 // Plain pass, launch 3 of 3: one CTA per tile writes the commands and
 // counts from the planes and the tile's carry.  No CTA waits for another.

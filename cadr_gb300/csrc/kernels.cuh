@@ -54,6 +54,7 @@ struct ViewJob {
     uint32_t* cmds;
     uint32_t* counts;
     uint32_t* marginal;
+    const uint32_t* tile_start;   // the scene's per-tile region starts (tiles of kLeafTile drawables)
     uint32_t n;
     uint32_t num_state_sets;
     uint32_t num_geometries;
@@ -67,6 +68,11 @@ struct ViewJob {
 constexpr int kLeafThreads = 256;
 constexpr int kLeafIpt = 8;
 constexpr int kLeafTile = kLeafThreads * kLeafIpt;
+constexpr int kLeafWarps = kLeafThreads / 32;
+// Write kernels: StateSet offsets staged in shared memory up to this many
+// entries; 40 registers give 6 CTAs per SM (5 and 8 measured slower).
+constexpr uint32_t kWriteOffsetCap = 4096;
+constexpr int kWriteCtasPerSm = 6;
 constexpr int kPropThreads = 256;
 
 // Internal level: world[i] = parent_world[parent[i]] * local[i].
@@ -132,12 +138,20 @@ cudaError_t launch_leaf_write(const LeafArgs& a, Scratch& s, cudaStream_t stream
 __host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 31) / 32 + 3) & ~uint64_t(3); }
 __host__ __device__ constexpr uint64_t leaf_plane_words(uint64_t n) { return 3 * leaf_plane_stride(n); }
 
-// Batched sphere cull: one persistent launch over all (view, tile) items.
+// Batched sphere cull over all (view, tile) items, in one of two forms
+// (cadr_tuning.form): kBatchedPersistent, one persistent launch of `grid`
+// CTAs with a decoupled lookback (scratch: s.ctl and s.tile_state for the
+// items); kBatchedThreeLaunch, classify / per-view tile scan / write with
+// tiles of kLeafTile drawables and no waits (scratch: s.planes of
+// batched_plane_words words).
+constexpr uint32_t kBatchedPersistent = 0, kBatchedThreeLaunch = 1;
 cudaError_t launch_batched_cull(const ViewJob* d_jobs, uint32_t num_jobs, uint32_t total_items,
                                 Scratch& s, uint32_t* error, uint64_t spin_limit_ns, uint32_t fault,
-                                uint32_t block_threads, uint32_t items_per_thread, uint32_t grid,
-                                cudaStream_t stream);
-uint32_t batched_tile(uint32_t block_threads, uint32_t items_per_thread);
+                                const cadr_tuning& tu, uint32_t grid, cudaStream_t stream);
+// Drawables per work item of a tuning.
+uint32_t batched_tile(const cadr_tuning& tu);
+// Plane words a batch of `total_items` items needs (0 for the persistent form).
+uint64_t batched_plane_words(const cadr_tuning& tu, uint64_t total_items);
 
 // Tier A.
 cudaError_t launch_process_drawables(uint32_t level, const uint64_t* root,

@@ -5,8 +5,8 @@
 // scheduler thread admits queued requests in arrival order while output
 // memory is available (first-fit in an output arena sized from free device
 // memory or the configured budget) and a batch slot is free, waits up to the
-// batching window for more requests to join, and launches the batch with
-// the batched persistent kernel on the slot's own stream and lookback
+// batching window for more requests to join, and launches the batch in
+// the batched form of the context's tuning on the slot's own stream and
 // scratch.  Several slots are in flight at once, so requests that arrive
 // while others run are admitted into the next slot and their work overlaps
 // on the device.  Completion is stamped by a host callback on the slot's
@@ -197,9 +197,10 @@ static cadr_status launch_slot(cadr_server* srv, Slot* slot, std::vector<Request
         }
     }
     uint64_t total = 0;
-    cadr_status st = build_jobs(bv.data(), nv, batched_tile(tu.block_threads, tu.items_per_thread), slot->h_jobs, &total);
+    cadr_status st = build_jobs(bv.data(), nv, batched_tile(tu), slot->h_jobs, &total);
     if (st != CADR_OK) return st;
     st = scratch_reserve(ctx, slot->scratch, total);
+    if (st == CADR_OK) st = scratch_reserve_planes(ctx, slot->scratch, batched_plane_words(tu, total));
     if (st != CADR_OK) return st;
     // Spread the device between the slots in flight.
     const uint32_t share = std::max<uint32_t>(1u, (uint32_t)srv->slots.size());
@@ -208,9 +209,9 @@ static cadr_status launch_slot(cadr_server* srv, Slot* slot, std::vector<Request
     e = cudaMemcpyAsync(slot->d_jobs, slot->h_jobs, nv * sizeof(ViewJob), cudaMemcpyHostToDevice, slot->stream);
     if (e == cudaSuccess)
         e = launch_batched_cull(slot->d_jobs, nv, (uint32_t)total, slot->scratch, ctx->d_error, ctx->spin_limit_ns,
-                                CADR_FAULT_NONE, tu.block_threads, tu.items_per_thread, grid, slot->stream);
+                                CADR_FAULT_NONE, tu, grid, slot->stream);
     if (e != cudaSuccess) return cuda_fail(e, "server: launch");
-    ctx->launches++;
+    ctx->launches += tu.form == kBatchedThreeLaunch ? 3 : 1;
     slot->scratch.launches++;
     slot->reqs = batch;
     e = cudaLaunchHostFunc(slot->stream, on_slot_done, slot);

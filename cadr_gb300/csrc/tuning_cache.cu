@@ -13,9 +13,9 @@
 // temporary file and renamed over the old one, so a reader never sees a
 // torn file (with several writers the last rename wins):
 //   {
-//    "version": 1,
+//    "version": 2,
 //    "entries": {
-//     "<key>": {"block_threads": 256, "items_per_thread": 8, "ctas_per_sm": 4, "ms": 0.7712},
+//     "<key>": {"block_threads": 256, "items_per_thread": 8, "ctas_per_sm": 4, "form": 0, "ms": 0.7712},
 //     ...
 //    }
 //   }
@@ -67,8 +67,11 @@ std::map<std::string, Entry> read_cache(const char* path)
         const char* body = std::strstr(q1, "\"block_threads\"");
         if (!body) continue;
         Entry e{};
-        if (std::sscanf(body, "\"block_threads\": %u, \"items_per_thread\": %u, \"ctas_per_sm\": %u, \"ms\": %f",
-                        &e.tuning.block_threads, &e.tuning.items_per_thread, &e.tuning.ctas_per_sm, &e.ms) == 4)
+        if (std::sscanf(body,
+                        "\"block_threads\": %u, \"items_per_thread\": %u, \"ctas_per_sm\": %u, \"form\": %u, "
+                        "\"ms\": %f",
+                        &e.tuning.block_threads, &e.tuning.items_per_thread, &e.tuning.ctas_per_sm, &e.tuning.form,
+                        &e.ms) == 5)
             out[std::string(q0 + 1, q1)] = e;
     }
     std::fclose(f);
@@ -80,12 +83,14 @@ bool write_cache(const char* path, const std::map<std::string, Entry>& entries)
     const std::string tmp = std::string(path) + ".tmp";
     FILE* f = std::fopen(tmp.c_str(), "w");
     if (!f) return false;
-    std::fprintf(f, "{\n \"version\": 1,\n \"entries\": {\n");
+    std::fprintf(f, "{\n \"version\": 2,\n \"entries\": {\n");
     size_t k = 0;
     for (const auto& kv : entries) {
         const cadr_tuning& t = kv.second.tuning;
-        std::fprintf(f, "  \"%s\": {\"block_threads\": %u, \"items_per_thread\": %u, \"ctas_per_sm\": %u, \"ms\": %.6f}%s\n",
-                     kv.first.c_str(), t.block_threads, t.items_per_thread, t.ctas_per_sm, kv.second.ms,
+        std::fprintf(f,
+                     "  \"%s\": {\"block_threads\": %u, \"items_per_thread\": %u, \"ctas_per_sm\": %u, "
+                     "\"form\": %u, \"ms\": %.6f}%s\n",
+                     kv.first.c_str(), t.block_threads, t.items_per_thread, t.ctas_per_sm, t.form, kv.second.ms,
                      ++k < entries.size() ? "," : "");
     }
     std::fprintf(f, " }\n}\n");
@@ -95,14 +100,16 @@ bool write_cache(const char* path, const std::map<std::string, Entry>& entries)
 
 }  // namespace
 
-// The combinations the autotuner tries, in search order.
+// The combinations the autotuner tries, in search order: every persistent
+// shape whose threads an SM holds, then the three-launch form.
 std::vector<cadr_tuning> tuning_candidates()
 {
     std::vector<cadr_tuning> out;
     for (uint32_t th : {128u, 256u, 512u})
         for (uint32_t ipt : {4u, 8u, 16u})
             for (uint32_t c : {2u, 4u, 8u})
-                if (th * c <= 2048) out.push_back(cadr_tuning{th, ipt, c, 0});  // threads an SM holds
+                if (th * c <= 2048) out.push_back(cadr_tuning{th, ipt, c, CADR_BATCHED_PERSISTENT});
+    out.push_back(cadr_tuning{256u, 8u, 4u, CADR_BATCHED_THREE_LAUNCH});
     return out;
 }
 

@@ -49,7 +49,10 @@ class BatchView(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_threads", u32), ("items_per_thread", u32), ("ctas_per_sm", u32),
-                ("reserved", u32)]
+                ("form", u32)]
+
+
+BATCHED_PERSISTENT, BATCHED_THREE_LAUNCH = 0, 1
 
 
 class MemoryRegion(C.Structure):
@@ -371,8 +374,8 @@ class Context:
         check(self.lib.cadr_get_tuning(self.handle, C.byref(t)))
         return t
 
-    def set_tuning(self, block_threads, items_per_thread, ctas_per_sm):
-        t = Tuning(block_threads, items_per_thread, ctas_per_sm, 0)
+    def set_tuning(self, block_threads, items_per_thread, ctas_per_sm, form=0):
+        t = Tuning(block_threads, items_per_thread, ctas_per_sm, form)
         check(self.lib.cadr_set_tuning(self.handle, C.byref(t)))
 
 

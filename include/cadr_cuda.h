@@ -451,11 +451,20 @@ typedef struct cadr_batch_view {
     uint32_t* marginal;           /* device or NULL */
 } cadr_batch_view;
 
+/* form 0 (CADR_BATCHED_PERSISTENT): one persistent launch over (view, tile)
+ * items of block_threads * items_per_thread drawables, compacting with a
+ * decoupled lookback between tiles; grid = ctas_per_sm * SMs.
+ * form 1 (CADR_BATCHED_THREE_LAUNCH): three launches (classify, a per-view
+ * scan of the tiles' counts, write) over tiles of 2,048 drawables with no
+ * waits between CTAs, as the plain pass; it takes block_threads 256 and
+ * items_per_thread 8.  Both give identical outputs. */
+#define CADR_BATCHED_PERSISTENT 0u
+#define CADR_BATCHED_THREE_LAUNCH 1u
 typedef struct cadr_tuning {
     uint32_t block_threads;       /* 128, 256, 512 */
-    uint32_t items_per_thread;    /* 1..16 */
-    uint32_t ctas_per_sm;         /* persistent grid = ctas_per_sm * SMs */
-    uint32_t reserved;
+    uint32_t items_per_thread;    /* 4, 8, 16 */
+    uint32_t ctas_per_sm;         /* persistent grid = ctas_per_sm * SMs, 1..16 */
+    uint32_t form;                /* CADR_BATCHED_* */
 } cadr_tuning;
 
 CADR_API cadr_status cadr_cull_batched(cadr_context* ctx, const cadr_batch_view* views,

@@ -37,7 +37,7 @@ def test_world_spheres_match_oracle(ctx, c4_small):
         ds.host  # keep alive
 
 
-@pytest.mark.parametrize("tuning", [None, (128, 4, 4), (512, 8, 2), (256, 16, 8)])
+@pytest.mark.parametrize("tuning", [None, (128, 4, 4), (512, 8, 2), (256, 16, 8), (256, 8, 4, 1)])
 def test_batched_equals_plain(ctx, c4_small, tuning):
     scs, dss = c4_small
     items, outs = [], []
@@ -48,7 +48,7 @@ def test_batched_equals_plain(ctx, c4_small, tuning):
             items.append((ds, v, o))
             outs.append((sc, ds, v, o))
     arr = lib.batch_views(items)
-    t = lib.Tuning(*tuning, 0) if tuning else None
+    t = lib.Tuning(*(tuning + (0,))[:4]) if tuning else None
     for _ in range(2):  # second call replays the captured graph
         lib.cull_batched(ctx, arr, t, use_graph=True)
         ctx.sync()
@@ -123,3 +123,66 @@ def test_batched_marginal_bits_equal_plain(ctx):
     got, ref = o.fetch(), _plain(ctx, sc, ds, sc.views[0])
     assert_same(got, ref, sc.state_set_offsets)
     assert np.unpackbits(got["marginal"].view(np.uint8)).sum() > 0.15 * sc.n
+
+
+@pytest.mark.parametrize("form", [lib.BATCHED_PERSISTENT, lib.BATCHED_THREE_LAUNCH])
+def test_batch_with_empty_and_ragged_scenes(ctx, form):
+    """Scenes of 0, 1, 2,047, 2,049 and 100,003 drawables (many StateSets,
+    some empty) in one batch, in both forms: each view equals its plain
+    pass, the empty scene's counts are zero."""
+    shapes = [(0, 4), (1, 1), (2047, 5), (2049, 300), (100_003, 64)]
+    items, outs = [], []
+    for k, (n, S) in enumerate(shapes):
+        sc = scenes.small_scene(seed=70 + k, n=n, num_levels=2 if n else 1, num_state_sets=S, num_lods=3,
+                                empty_state_sets=(1,) if S > 2 else ())
+        ds = lib.DeviceScene(ctx, sc)
+        ds.propagate(world_spheres=True)
+        for v in range(2):
+            view = sc.views[0] if v == 0 else scenes.random_view(9, k)
+            o = lib.CullOutputs(ctx, n, S)
+            ctx.upload(o.counts, np.full(S, 77, np.uint32))
+            items.append((ds, view, o))
+            outs.append((sc, ds, view, o))
+    lib.cull_batched(ctx, lib.batch_views(items), lib.Tuning(256, 8, 4, form), use_graph=False)
+    ctx.sync()
+    ctx.check_device_error()
+    for sc, ds, view, o in outs:
+        got = o.fetch()
+        if sc.n == 0:
+            assert (got["counts"] == 0).all()
+            continue
+        assert_same(got, _plain(ctx, sc, ds, view), sc.state_set_offsets)
+
+
+def test_server_in_the_three_launch_form(ctx, c4_small):
+    """The serving loop batches with the context's tuning: in the
+    three-launch form its results equal the plain passes."""
+    scs, dss = c4_small
+    saved = ctx.get_tuning()
+    ctx.set_tuning(256, 8, 4, lib.BATCHED_THREE_LAUNCH)
+    try:
+        srv = lib.Server(ctx, max_inflight=2, max_batch_views=8, window_ns=100_000)
+        reqs = {}
+        for k in range(12):
+            si = k % len(scs)
+            views = np.concatenate([scenes.random_view(6, 10 * k + j) for j in range(1 + k % 3)])
+            reqs[srv.submit(dss[si], views)] = (si, views)
+        srv.drain()
+        done = {r.request_id: r for r in srv.poll()}
+        assert set(done) == set(reqs)
+        for rid, (si, views) in reqs.items():
+            r = done[rid]
+            assert r.status == lib.OK
+            for v in range(len(views)):
+                counts = ctx.download(r.counts[v], np.uint32, (scs[si].num_state_sets,))
+                cmds = ctx.download(r.cmds[v], scenes.CMD_DTYPE, (scs[si].n,))
+                ref = _plain(ctx, scs[si], dss[si], views[v:v + 1])
+                assert np.array_equal(counts, ref["counts"])
+                off = scs[si].state_set_offsets
+                assert np.array_equal(bind.valid_cmds(cmds, counts, off).view(np.uint8),
+                                      bind.valid_cmds(ref["cmds"], ref["counts"], off).view(np.uint8))
+            srv.release(rid)
+        srv.close()
+    finally:
+        ctx.set_tuning(saved.block_threads, saved.items_per_thread, saved.ctas_per_sm, saved.form)
+
