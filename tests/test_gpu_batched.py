@@ -130,7 +130,10 @@ def test_batch_with_empty_and_ragged_scenes(ctx, form):
     """Scenes of 0, 1, 2,047, 2,049 and 100,003 drawables (many StateSets,
     some empty) in one batch, in both forms: each view equals its plain
     pass, the empty scene's counts are zero."""
-    shapes = [(0, 4), (1, 1), (2047, 5), (2049, 300), (100_003, 64)]
+    # The last two have more StateSets than either form stages in shared
+    # memory (2,048 offsets for the persistent form, 4,096 for the write
+    # kernel of the three-launch form).
+    shapes = [(0, 4), (1, 1), (2047, 5), (2049, 300), (100_003, 64), (30_000, 3000), (40_000, 5000)]
     items, outs = [], []
     for k, (n, S) in enumerate(shapes):
         sc = scenes.small_scene(seed=70 + k, n=n, num_levels=2 if n else 1, num_state_sets=S, num_lods=3,

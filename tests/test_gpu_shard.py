@@ -37,6 +37,7 @@ def _assert_merged_equal(merged_cmds, counts, ref, offsets):
     (100_003, 2, 5, ()),              # ragged tiles at both shard ends
     (5000, 4, 3000, ()),              # more regions than drawables per shard
     (2048 * 3, 3, 2, (0,)),           # shard boundaries on tile boundaries
+    (60_000, 2, 5000, (7, 4999)),     # more StateSets than the write kernel stages in shared memory
 ])
 def test_shards_merge_to_the_single_rank_pass(ctx, n, world, S, empty):
     sc = scenes.small_scene(seed=n + world, n=n, num_levels=2, num_state_sets=S, num_lods=3,
