@@ -1,4 +1,5 @@
-"""ctypes binding of oracle/_build/libcadr_oracle.so and oracle/_ref/libcadr_ref.so.
+"""ctypes binding of oracle/_build/libcadr_oracle.so, oracle/_ref/libcadr_ref.so
+and oracle/_ref/libcadr_ref_shader.so.
 
 TEST INFRASTRUCTURE ONLY (see oracle/__init__.py).
 """
@@ -13,6 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcadr_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libcadr_ref.so")
+REF_SHADER_PATH = os.path.join(HERE, "_ref", "libcadr_ref_shader.so")
 
 
 def reference_root() -> str:
@@ -29,6 +31,7 @@ def reference_root() -> str:
 
 _lib = None
 _ref = None
+_ref_shader = None
 
 
 def build(with_ref: bool = True) -> None:
@@ -83,6 +86,54 @@ def load_ref():
         _ref.ref_sphere_transform.argtypes = [C.c_void_p] * 3
         _ref.ref_glm_version.restype = C.c_int
     return _ref
+
+
+def load_ref_shader():
+    """The reference's processDrawables shader compiled as C++
+    (ref_shader_shim.h, ref_shader_harness.cpp), or None when it was not
+    built (it needs the CADR sources)."""
+    global _ref_shader
+    if _ref_shader is None and os.path.exists(REF_SHADER_PATH):
+        L = C.CDLL(REF_SHADER_PATH)
+        u32, u64 = C.c_uint32, C.c_uint64
+        L.cadr_ref_shader_process.argtypes = [u32, u64, u64, u64, u64, u64]
+        L.cadr_ref_shader_process.restype = C.c_int
+        L.cadr_ref_shader_map.argtypes = [u64, u64]
+        L.cadr_ref_shader_map.restype = C.c_int
+        L.cadr_ref_shader_unmap.argtypes = [u64, u64]
+        L.cadr_ref_shader_unmap.restype = C.c_int
+        _ref_shader = L
+    return _ref_shader
+
+
+def ref_shader_process_drawables(image: np.ndarray, image_base: int, handle_level: int, root: int,
+                                 drawables: np.ndarray):
+    """Runs the reference's shader over a memory image laid out for
+    image_base (256-byte aligned, as Tier A images are): the image is copied
+    to host memory mapped at exactly that address, one shader invocation runs
+    per drawable, and the mapping is removed.  The shader dereferences the
+    addresses its tables hold, so the image must hold every PrimitiveSet and
+    MatrixList the drawables reach.  Returns (indirect uint32 [N,4], pointers
+    uint64 [N,4]), or None when the address range is not free."""
+    L = load_ref_shader()
+    if L is None:
+        raise RuntimeError("oracle/_ref/libcadr_ref_shader.so is not built (make -C oracle ref)")
+    size = max(int(image.nbytes), 1)
+    size = (size + 4095) & ~4095
+    if L.cadr_ref_shader_map(image_base, size) != 0:
+        return None
+    try:
+        C.memmove(image_base, image.ctypes.data, int(image.nbytes))
+        d = np.ascontiguousarray(drawables)
+        n = int(d.shape[0])
+        ind = np.zeros((n, 4), np.uint32)
+        ptr = np.zeros((n, 4), np.uint64)
+        rc = L.cadr_ref_shader_process(handle_level, root, d.ctypes.data, n, ind.ctypes.data, ptr.ctypes.data)
+        if rc != 0:
+            raise ValueError("cadr_ref_shader_process: handle level %d" % handle_level)
+        return ind, ptr
+    finally:
+        L.cadr_ref_shader_unmap(image_base, size)
 
 
 def max_threads() -> int:

@@ -10,8 +10,12 @@
                 outputs, so GPU tests can check against stored bits.
   c1.json       hashes of the C1 inputs (generator reproducibility) and of
                 the oracle's C1 outputs.
-  tier_a.json   hashes of the oracle's Tier A outputs on three images
-                (handle-table depths 1, 2, 3).
+  tier_a.json   hashes of the Tier A outputs on three images (handle-table
+                depths 1, 2, 3), computed by the reference's own
+                processDrawables shader (src/CadR/shaders/processDrawables.comp)
+                compiled as C++ into oracle/_ref by `make -C oracle ref`
+                (oracle/ref_shader_shim.h); the oracle must give the same
+                bits before they are written.
 
 Run from the repository root in the build container (the reference sources
 must be present):  python tests/golden/make_golden.py
@@ -93,11 +97,17 @@ def tier_a_summary():
                      "level2": dict(n=5000),
                      "level3": dict(n=3000, num_geometries=50, extra_handles=4_200_000)}.items():
         im = tier_a.build(seed=7, base=TIER_A_BASE, **kw)
-        ind, ptr = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables, threads=1)
+        ref = bind.ref_shader_process_drawables(im.image, im.base, im.level, im.root, im.drawables)
+        assert ref is not None, "address range of the Tier A image is taken"
+        ind, ptr = ref
+        o_ind, o_ptr = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables, threads=1)
+        assert np.array_equal(o_ind, ind) and np.array_equal(o_ptr, ptr), name
         res[name] = {"kwargs": kw, "level": im.level, "image": sha(im.image), "drawables": sha(im.drawables),
                      "indirect": sha(ind), "pointers": sha(ptr)}
     with open(os.path.join(HERE, "tier_a.json"), "w") as f:
-        json.dump({"base": TIER_A_BASE, "seed": 7, "images": res}, f, indent=1)
+        json.dump({"base": TIER_A_BASE, "seed": 7,
+                   "computed_by": "src/CadR/shaders/processDrawables.comp compiled as C++ (oracle/ref_shader_shim.h)",
+                   "images": res}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -124,10 +124,9 @@ def test_tier_a_golden(oracle_lib):
 # ---------------------------------------------------------------------------
 # Known answers derived by hand from processDrawables.comp:77-113.
 
-def _hand_image(level):
-    """A hand-laid memory image: base 0x100000, handle table of `level` levels,
+def _hand_image(level, base=0x100000):
+    """A hand-laid memory image at `base`, handle table of `level` levels,
     one PrimitiveSet array and one MatrixList."""
-    base = 0x100000
     img = np.zeros(0x40000, np.uint8)
     u64 = img.view(np.uint64)
     u32 = img.view(np.uint32)
@@ -186,6 +185,68 @@ def test_tier_a_known_answers(oracle_lib, level):
     ml = base + 0x30100
     # handle 0 resolves through entry 0 of the tables, which is 0
     assert ptr.tolist() == [[0xAAAA0000, 0xBBBB0000, ml, 0xCCCC0000], [0xAAAA0000, 0xBBBB0000, ml, 0]]
+
+
+# ---------------------------------------------------------------------------
+# The reference's processDrawables shader itself, compiled as C++ from the
+# CADR sources (oracle/ref_shader_shim.h); only where they are present, i.e.
+# in the build container.
+
+def _ref_shader():
+    from oracle import bind
+    if bind.load_ref_shader() is None:
+        pytest.skip("reference shader not built (needs the CADR sources)")
+    return bind
+
+
+REF_BASE = 0x7E0000000000
+
+
+def test_tier_a_reference_shader_golden(oracle_lib):
+    """The golden Tier A hashes are the reference shader's outputs."""
+    bind = _ref_shader()
+    d = json.load(open(os.path.join(GOLDEN, "tier_a.json")))
+    for name, e in d["images"].items():
+        im = tier_a.build(seed=d["seed"], base=d["base"], **e["kwargs"])
+        r = bind.ref_shader_process_drawables(im.image, im.base, im.level, im.root, im.drawables)
+        if r is None:
+            pytest.skip("address range of the golden images is taken in this process")
+        assert sha(r[0]) == e["indirect"], name
+        assert sha(r[1]) == e["pointers"], name
+
+
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_tier_a_reference_shader_known_answers(oracle_lib, level):
+    bind = _ref_shader()
+    img, base, root, d = _hand_image(level, base=REF_BASE)
+    r = bind.ref_shader_process_drawables(img, base, level, root, d)
+    if r is None:
+        pytest.skip("address range taken in this process")
+    ind, ptr = r
+    assert ind.tolist() == [[11, 7, 100, 0], [33, 7, 300, 0]]
+    ml = base + 0x30100
+    assert ptr.tolist() == [[0xAAAA0000, 0xBBBB0000, ml, 0xCCCC0000], [0xAAAA0000, 0xBBBB0000, ml, 0]]
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n=1, num_geometries=1),
+    dict(n=777, prims_per_geometry=7, matrices_per_list=3),
+    dict(n=2500, with_drawable_data=False),
+    dict(n=1200, num_geometries=40, geometry_data=True),
+    dict(n=900, num_geometries=30, extra_handles=2048 * 2048),
+])
+def test_tier_a_oracle_matches_reference_shader(oracle_lib, kw):
+    """The oracle against the reference shader on images of each handle-table
+    depth, with several PrimitiveSet counts, MatrixList sizes and without
+    drawable data (handle 0)."""
+    bind = _ref_shader()
+    im = tier_a.build(seed=31, base=REF_BASE, **kw)
+    r = bind.ref_shader_process_drawables(im.image, im.base, im.level, im.root, im.drawables)
+    if r is None:
+        pytest.skip("address range taken in this process")
+    o = bind.process_drawables(im.image, im.base, im.level, im.root, im.drawables, threads=2)
+    assert np.array_equal(o[0], r[0])
+    assert np.array_equal(o[1], r[1])
 
 
 def test_tier_a_out_of_image_is_reported(oracle_lib):
