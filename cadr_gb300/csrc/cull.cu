@@ -44,8 +44,8 @@ __device__ __forceinline__ uint32_t xpose_pos(uint32_t q) { return q ^ ((q >> 3)
 // and, with kCull, the classification.  Item j of thread t is drawable
 // b + j*kLeafThreads + t, i.e. lane t%32 of row j of warp t/32; xb is the
 // warp's staging block.  With kCull, row j's visibility ballot goes to
-// ballot[j][warp] and, with the LOD bits and the marginal flags, to the
-// planes (one word per 32 drawables).
+// ballot[j][warp] and, with the LOD bits, to word 8 warp + j of the tile's
+// 64 in each plane; the marginal flags go out in drawable order.
 template <bool kCull>
 __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint32_t (*ballot)[kLeafWarps],
                                             float4* xb)
@@ -127,9 +127,10 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint3
                 ballot[j][warp] = vb;
                 if (i0 < a.n) {
                     const uint32_t w = i0 >> 5;
-                    a.planes[w] = vb;
-                    a.planes[words + w] = lb0;
-                    a.planes[2 * words + w] = lb1;
+                    const uint32_t wt = (i0 >> 11) * 64u + (uint32_t)warp * 8u + (uint32_t)j;
+                    a.planes[wt] = vb;
+                    a.planes[words + wt] = lb0;
+                    a.planes[2 * words + wt] = lb1;
                     if (a.marginal) a.marginal[w] = mb;
                 }
             }
@@ -185,7 +186,8 @@ __global__ void __launch_bounds__(kScanThreads) leaf_tile_scan_kernel(uint32_t* 
 // It is launched as a programmatic dependent of the tile scan: everything
 // but the carry (the planes, the geometry ids, the offsets, the LOD-table
 // gathers) is loaded while the scan still runs, and only the carry is read
-// after griddepcontrol.wait.  The loads are independent of one another,
+// after griddepcontrol.wait.  A warp's 8 row words of a plane are two
+// 16-byte loads.  The loads are independent of one another,
 // so a tile costs about two memory round trips.  With kShard (a shard of a
 // pass split over devices) the commands are placed by a.shard and the
 // counts, written by the region-count kernel before, are left alone.
@@ -199,13 +201,20 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     const uint32_t stride = (uint32_t)leaf_plane_stride(a.n);
     const uint32_t* off = stage_offsets(s_off, a.off_cap, a.offsets, a.num_state_sets);
     uint32_t vw[kLeafIpt], l0[kLeafIpt], l1[kLeafIpt], geo[kLeafIpt];
+    {
+        const uint4* pv = reinterpret_cast<const uint4*>(a.planes + tile * 64u + (uint32_t)warp * 8u);
+        const uint32_t q = stride / 4u;
+        const uint4 v0 = __ldg(pv), v1 = __ldg(pv + 1), a0 = __ldg(pv + q), a1 = __ldg(pv + q + 1),
+                    c0 = __ldg(pv + 2 * q), c1 = __ldg(pv + 2 * q + 1);
+        vw[0] = v0.x; vw[1] = v0.y; vw[2] = v0.z; vw[3] = v0.w; vw[4] = v1.x; vw[5] = v1.y; vw[6] = v1.z; vw[7] = v1.w;
+        l0[0] = a0.x; l0[1] = a0.y; l0[2] = a0.z; l0[3] = a0.w; l0[4] = a1.x; l0[5] = a1.y; l0[6] = a1.z; l0[7] = a1.w;
+        l1[0] = c0.x; l1[1] = c0.y; l1[2] = c0.z; l1[3] = c0.w; l1[4] = c1.x; l1[5] = c1.y; l1[6] = c1.z; l1[7] = c1.w;
+    }
 #pragma unroll
     for (int j = 0; j < kLeafIpt; j++) {
         const uint32_t i0 = b + (uint32_t)(j * kLeafThreads + warp * kWarp);
         const uint32_t i = i0 + (uint32_t)lane;
-        vw[j] = i0 < a.n ? __ldg(a.planes + (i0 >> 5)) : 0u;
-        l0[j] = i0 < a.n ? __ldg(a.planes + stride + (i0 >> 5)) : 0u;
-        l1[j] = i0 < a.n ? __ldg(a.planes + 2 * stride + (i0 >> 5)) : 0u;
+        if (i0 >= a.n) vw[j] = l0[j] = l1[j] = 0u;
         geo[j] = i < a.n ? __ldg(a.geometry + i) : 0u;
     }
     uint32_t vis_bits = 0, lod_bits = 0;
@@ -252,7 +261,9 @@ __global__ void __launch_bounds__(256) leaf_region_count_kernel(const uint32_t* 
             base = __ldg(carries + last_tile);
         }
         for (uint32_t w = (from >> 5) + lane; w <= ((e - 1) >> 5); w += 32u) {
-            uint32_t v = __ldg(planes + w);
+            // word w in drawable order (tile, row j, warp) is stored at
+            // tile word 8 warp + j
+            uint32_t v = __ldg(planes + ((w & ~63u) | ((w & 7u) << 3) | ((w >> 3) & 7u)));
             const uint32_t lo = w * 32u;
             if (from > lo) v &= ~0u << (from - lo);      // from - lo in 1..31
             if (e < lo + 32u) v &= (1u << (e - lo)) - 1u;  // e - lo in 1..31

@@ -134,8 +134,11 @@ cudaError_t launch_leaf_stream_scan(const LeafArgs& a, Scratch& s, cudaStream_t 
                                     bool after_level_kernel);
 cudaError_t launch_leaf_region_counts(const LeafArgs& a, Scratch& s, cudaStream_t stream);
 cudaError_t launch_leaf_write(const LeafArgs& a, Scratch& s, cudaStream_t stream, bool after_scan);
-// Words of one bit-plane (one per 32 drawables), padded to 16 bytes.
-__host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 31) / 32 + 3) & ~uint64_t(3); }
+// Words of one bit-plane: one per 32 drawables, 64 per tile of kLeafTile
+// drawables.  Inside a tile, word 8 w + j holds row j of warp w (drawables
+// 256 j + 32 w .. + 31 of the tile), so that the 8 words a warp of the
+// write kernel reads are 32 contiguous bytes.
+__host__ __device__ constexpr uint64_t leaf_plane_stride(uint64_t n) { return ((n + 2047) / 2048) * 64; }
 __host__ __device__ constexpr uint64_t leaf_plane_words(uint64_t n) { return 3 * leaf_plane_stride(n); }
 
 // Batched sphere cull over all (view, tile) items, in one of two forms
