@@ -42,32 +42,28 @@ namespace {
 // up to this many entries (8 KiB).
 constexpr uint32_t kBatchedOffsetCap = 2048;
 
-// The job of work item `item`: items only grow within a CTA, so the job is
-// at or after `from`.  Gallop forward, then bisect.
-__device__ __forceinline__ uint32_t find_job(const ViewJob* __restrict__ jobs, uint32_t num_jobs, uint32_t from,
-                                             uint32_t item)
+// The job of work item `item`, found by one warp: each round its lanes
+// probe 32 evenly spaced jobs and keep the last whose first item is at or
+// below `item` (two rounds up to 1,024 jobs).  jobs[0].first_item is 0.
+__device__ __forceinline__ uint32_t warp_find_job(const ViewJob* __restrict__ jobs, uint32_t num_jobs, uint32_t item)
 {
-    uint32_t lo = from, hi = lo + 1, step = 1;
-    while (hi < num_jobs && __ldg(&jobs[hi].first_item) <= item) {
-        lo = hi;
-        step <<= 1;
-        hi = lo + step;
-    }
-    hi = min(hi, num_jobs);
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo = 0, hi = num_jobs;  // the job is in [lo, hi); jobs[lo].first_item <= item
     while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&jobs[mid].first_item) <= item)
-            lo = mid;
-        else
-            hi = mid;
+        const uint32_t step = (hi - lo + 31u) / 32u;
+        const uint32_t k = lo + lane * step;
+        const uint32_t m = __ballot_sync(~0u, k < hi && __ldg(&jobs[k].first_item) <= item);
+        lo += (31u - (uint32_t)__clz(m)) * step;  // lane 0 always holds: bit 0 is set
+        hi = min(hi, lo + step);
     }
     return lo;
 }
 
-// The persistent kernel.  Per item: thread 0 publishes the item (and its
-// job) by the first barrier; load and classify, barrier; warp 0 scans the
-// tile, publishes the tile's aggregate and looks back while the other
-// warps gather their LOD entries, barrier; write.  The per-item tile state
+// The persistent kernel.  Per item: warp 0 publishes the item (lane 0
+// takes it) and its job (the warp's two-round search) by the first
+// barrier; load and classify, barrier; warp 0 scans the tile, publishes
+// the tile's aggregate and looks back while the other warps gather their
+// LOD entries, barrier; write.  The per-item tile state
 // is double-buffered (item k uses sm[k & 1]), so the next item's ballots
 // never overwrite what a slower warp still reads in this item's write
 // phase, and the first barrier of the next item, which every thread
@@ -78,7 +74,9 @@ __device__ __forceinline__ uint32_t find_job(const ViewJob* __restrict__ jobs, u
 // Launch bounds of 1,024 threads per SM cap the kernel at 64 registers:
 // at 80 (unbounded) only three 256-thread CTAs fit an SM and the item chain
 // of each has fewer neighbours to hide behind; capped, four fit, and C4 ran
-// 0.737 -> 0.671 ms (a 24-byte spill at 8 items per thread).
+// 0.737 -> 0.671 ms (a 24-byte spill at 8 items per thread).  The job
+// search by the whole warp (two dependent rounds) and the branch-free
+// plane tests of classify() took it to 0.657 ms.
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batched_kernel(const ViewJob* __restrict__ jobs, uint32_t num_jobs,
                                                          uint32_t total_items, const Scratch s, uint32_t* error,
@@ -101,10 +99,15 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batched_kernel(const 
     uint32_t nxt = 0;
     bool have_next = false;
     for (;;) {
-        if (t == 0) {
-            const uint32_t item = have_next ? nxt : atomicAdd(&s.ctl->tile_counter, 1u);
-            s_item = item;
-            s_job = find_job(jobs, num_jobs, cur_job == 0xffffffffu ? 0u : cur_job, item);
+        if (warp == 0) {
+            uint32_t it = 0;
+            if (lane == 0) it = have_next ? nxt : atomicAdd(&s.ctl->tile_counter, 1u);
+            it = __shfl_sync(~0u, it, 0);
+            const uint32_t jb = it < total_items ? warp_find_job(jobs, num_jobs, it) : 0u;
+            if (lane == 0) {
+                s_item = it;
+                s_job = jb;
+            }
         }
         __syncthreads();
         const uint32_t item = s_item;
@@ -179,23 +182,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batched_kernel(const 
 // kLeafTile drawables, so that each scene's per-tile region-start table
 // serves it.  No CTA waits for another: a reduce-then-scan like the plain
 // pass, with every view's first tile a scan head.
-
-// The job of work item `item`, found by one warp: each round its lanes
-// probe 32 evenly spaced jobs and keep the last whose first item is at or
-// below `item` (two rounds up to 1,024 jobs).  jobs[0].first_item is 0.
-__device__ __forceinline__ uint32_t warp_find_job(const ViewJob* __restrict__ jobs, uint32_t num_jobs, uint32_t item)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t lo = 0, hi = num_jobs;  // the job is in [lo, hi); jobs[lo].first_item <= item
-    while (hi - lo > 1) {
-        const uint32_t step = (hi - lo + 31u) / 32u;
-        const uint32_t k = lo + lane * step;
-        const uint32_t m = __ballot_sync(~0u, k < hi && __ldg(&jobs[k].first_item) <= item);
-        lo += (31u - (uint32_t)__clz(m)) * step;  // lane 0 always holds: bit 0 is set
-        hi = min(hi, lo + step);
-    }
-    return lo;
-}
 
 // Words of one bit-plane of a batch: 64 per item (2,048 drawables), padded
 // to 16 bytes.  Three planes (visibility, LOD bits 0 and 1), then one tile

@@ -262,8 +262,9 @@ __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, ui
     for (int p = 0; p < 6; p++) {
         const float4 pl = v.plane[p];
         const float dist = fadd(fadd(fadd(fmul(pl.x, ws.x), fmul(pl.y, ws.y)), fmul(pl.z, ws.z)), pl.w);
-        vis = vis && (dist >= nr);
-        mar = mar || (fabsf(fadd(dist, ws.w)) <= kMarginalBand);
+        // bitwise, not short-circuit: every plane test runs, branch-free
+        vis &= (dist >= nr);
+        mar |= (fabsf(fadd(dist, ws.w)) <= kMarginalBand);
     }
     float zc = 1.0f;
     if (v.perspective) {
@@ -277,7 +278,7 @@ __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, ui
     const float th[3] = {v.lod_threshold.x, v.lod_threshold.y, v.lod_threshold.z};
 #pragma unroll
     for (int k = 2; k >= 0; k--)
-        if ((uint32_t)k + 1 < num_lods && s >= fmul(th[k], zc)) l = (uint32_t)k;
+        if (((uint32_t)k + 1 < num_lods) & (s >= fmul(th[k], zc))) l = (uint32_t)k;
     visible = vis;
     marginal = mar;
     lod = l;
