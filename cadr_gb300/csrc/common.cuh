@@ -299,6 +299,23 @@ __device__ __forceinline__ uint32_t region_of(const uint32_t* offsets, uint32_t 
     return lo - 1;
 }
 
+// region_of(offsets, 0, S + 1, key) by a whole warp (every lane returns
+// it): a 32-way search, two rounds up to 1,024 entries.  offsets[0] is 0,
+// so the answer is at least 0.
+__device__ __forceinline__ uint32_t warp_region_of(const uint32_t* offsets, uint32_t S, uint32_t key)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo = 0, hi = S + 1;  // the answer is in [lo, hi); offsets[lo] <= key
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31u) / 32u;
+        const uint32_t k = lo + lane * step;
+        const uint32_t m = __ballot_sync(~0u, k < hi && offsets[k] <= key);
+        lo += (31u - (uint32_t)__clz(m)) * step;  // lane 0 always holds
+        hi = min(hi, lo + step);
+    }
+    return lo;
+}
+
 // Stages the S+1 StateSet offsets into shared memory when they fit `cap`
 // entries (all threads of the CTA call it; the caller's next
 // __syncthreads() publishes them) and returns the array to search.

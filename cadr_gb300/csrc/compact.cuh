@@ -134,8 +134,8 @@ struct Tile {
 
     // Warp 0 alone, after the ballots are stored and a __syncthreads(): the
     // same results as scan() (ballot-count prefix, total, the regions of
-    // the tile's first and last drawable, lanes 0 and 1 searching at once),
-    // with no CTA barrier; warp 0 sees them after its own __syncwarp(), the
+    // the tile's first and last drawable, each found by the whole warp in
+    // 32-way rounds), with no CTA barrier; warp 0 sees them after its own __syncwarp(), the
     // other warps after the caller's next __syncthreads().
     __device__ static __forceinline__ void scan_warp0(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
                                                       uint32_t b, uint32_t n)
@@ -164,13 +164,16 @@ struct Tile {
             run += c[k];
         }
         if (lane == 31) sm.info[3] = incl;
-        if (lane < 2) {
+        {
             // Clamped to S-1 so that an empty scene (n == 0, one work item)
             // stays inside the offsets and counts arrays.
             const uint32_t e = min(b + (uint32_t)SIZE, n);
-            const uint32_t key = lane == 0 ? b : (n ? e - 1 : 0u);
-            const uint32_t r = (lane == 1 && !n) ? S - 1 : min(region_of(offsets, 0, S + 1, key), S - 1);
-            sm.info[4 + lane] = r;
+            const uint32_t rf = min(warp_region_of(offsets, S, b), S - 1);
+            const uint32_t rl = n ? min(warp_region_of(offsets, S, e - 1), S - 1) : S - 1;
+            if (lane == 0) {
+                sm.info[4] = rf;
+                sm.info[5] = rl;
+            }
         }
         __syncwarp();
     }
