@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) batched_write_k
     const uint32_t tile = item - J->first_item;
     const uint32_t b = tile * (uint32_t)kLeafTile;
     const uint32_t* off = stage_offsets(s_off, kWriteOffsetCap, J->offsets, S);
+    if (t == 0 && n) cp_async_8(&sm.info[4], J->tile_region + tile);
     const uint32_t* geometry = J->geometry;
     const uint64_t base = (uint64_t)item * 64;
     uint32_t vw[kLeafIpt], l0[kLeafIpt], l1[kLeafIpt], geo[kLeafIpt];
@@ -299,9 +300,15 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) batched_write_k
     uint4 ent[kLeafIpt];
     LeafTile::gather(vis_bits, lod_bits, geo, J->lods, J->num_geometries, J->num_lods, error, ent);
     grid_dependency_wait();
-    if (t == 0) sm.info[2] = load_relaxed_u32(planes + 3 * stride + item);
+    if (t == 0) {
+        sm.info[2] = load_relaxed_u32(planes + 3 * stride + item);
+        cp_async_wait_all();
+    }
     __syncthreads();
-    LeafTile::scan(sm, off, S, b, n);
+    if (n)
+        LeafTile::scan_known_regions(sm);
+    else
+        LeafTile::scan(sm, off, S, b, n);
     LeafTile::write_ent(sm, vis_bits, ent, b, n, tile == 0, off, S, J->cmds, J->counts, error);
 }
 
@@ -413,6 +420,7 @@ cadr_status build_jobs(const cadr_batch_view* views, uint32_t n, uint32_t tile, 
         j.counts = bv.counts;
         j.marginal = bv.marginal;
         j.tile_start = sc->tile_start;
+        j.tile_region = reinterpret_cast<const uint2*>(sc->tile_region);
         j.n = (uint32_t)sc->desc.num_drawables;
         j.num_state_sets = sc->desc.num_state_sets;
         j.num_geometries = sc->desc.num_geometries;

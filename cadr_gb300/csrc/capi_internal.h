@@ -63,6 +63,8 @@ struct cadr_scene {
     std::vector<uint32_t> h_offsets;       // host copy of the StateSet offsets
     std::vector<uint32_t> h_tile_start;    // per leaf tile: start of the region of its last drawable
     uint32_t* tile_start = nullptr;        // device copy of h_tile_start (in the arena)
+    std::vector<uint32_t> h_tile_region;   // per leaf tile: regions of its first and last drawable
+    uint32_t* tile_region = nullptr;       // device copy of h_tile_region (in the arena)
     bool committed = false;
     bool upload_pending = false;
     cudaEvent_t uploaded = nullptr;

@@ -167,6 +167,15 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 // async-proxy (TMA) accesses of that memory.
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Asynchronous 8-byte copy global -> shared (both 8-byte aligned), with no
+// register holding the value; cp_async_wait_all() waits for this thread's
+// copies.
+__device__ __forceinline__ void cp_async_8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Bulk (TMA) prefetch of [src, src + bytes) into L2; 16-byte aligned
 // address, bytes % 16 == 0.  Brings a whole tile's stream on its way with
 // one instruction and no registers.

@@ -76,7 +76,7 @@ struct Tile {
     static constexpr int SIZE = THREADS * IPT;
     static_assert(NW >= 2, "two warps at least");
 
-    struct Smem {
+    struct __align__(16) Smem {
         uint32_t ballot[IPT][NW];
         uint32_t prefix[NC];
         uint32_t info[8];  // 0 item, 1 epoch, 2 carry, 3 total, 4 first region, 5 last region,
@@ -91,54 +91,9 @@ struct Tile {
         return sm.prefix[j * NW + w] + __popc(sm.ballot[j][w] & ((1u << l) - 1u));
     }
 
-    // After all ballots are stored and a __syncthreads(): scan the ballot
-    // counts (warp 0) and locate the regions of the tile's first and last
-    // drawable (warp 1).  Ends with __syncthreads().
-    __device__ static __forceinline__ void scan(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
-                                                uint32_t b, uint32_t n)
-    {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (warp == 0) {
-            constexpr int PER = (NC + 31) / 32;
-            uint32_t c[PER];
-            uint32_t sum = 0;
-#pragma unroll
-            for (int k = 0; k < PER; k++) {
-                const int idx = lane * PER + k;
-                c[k] = idx < NC ? __popc(sm.ballot[idx / NW][idx % NW]) : 0u;
-                sum += c[k];
-            }
-            uint32_t incl = sum;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(~0u, incl, o);
-                if (lane >= o) incl += v;
-            }
-            uint32_t run = incl - sum;
-#pragma unroll
-            for (int k = 0; k < PER; k++) {
-                const int idx = lane * PER + k;
-                if (idx < NC) sm.prefix[idx] = run;
-                run += c[k];
-            }
-            if (lane == 31) sm.info[3] = incl;
-        } else if (warp == 1 && lane == 0) {
-            // Clamped to S-1 so that an empty scene (n == 0, one work item)
-            // stays inside the offsets and counts arrays.
-            const uint32_t e = min(b + (uint32_t)SIZE, n);
-            sm.info[4] = min(region_of(offsets, 0, S + 1, b), S - 1);
-            sm.info[5] = n ? min(region_of(offsets, 0, S + 1, e - 1), S - 1) : S - 1;
-        }
-        __syncthreads();
-    }
-
-    // Warp 0 alone, after the ballots are stored and a __syncthreads(): the
-    // same results as scan() (ballot-count prefix, total, the regions of
-    // the tile's first and last drawable, each found by the whole warp in
-    // 32-way rounds), with no CTA barrier; warp 0 sees them after its own __syncwarp(), the
-    // other warps after the caller's next __syncthreads().
-    __device__ static __forceinline__ void scan_warp0(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
-                                                      uint32_t b, uint32_t n)
+    // Warp 0: the exclusive prefix of the ballot counts (prefix[]) and the
+    // tile's total (info[3]).
+    __device__ static __forceinline__ void prefix_warp0(Smem& sm)
     {
         const int lane = threadIdx.x & 31;
         constexpr int PER = (NC + 31) / 32;
@@ -164,16 +119,55 @@ struct Tile {
             run += c[k];
         }
         if (lane == 31) sm.info[3] = incl;
-        {
+    }
+
+    // After all ballots are stored and a __syncthreads(): scan the ballot
+    // counts (warp 0) and locate the regions of the tile's first and last
+    // drawable (warp 1).  Ends with __syncthreads().
+    __device__ static __forceinline__ void scan(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
+                                                uint32_t b, uint32_t n)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (warp == 0) {
+            prefix_warp0(sm);
+        } else if (warp == 1 && lane == 0) {
             // Clamped to S-1 so that an empty scene (n == 0, one work item)
             // stays inside the offsets and counts arrays.
             const uint32_t e = min(b + (uint32_t)SIZE, n);
-            const uint32_t rf = min(warp_region_of(offsets, S, b), S - 1);
-            const uint32_t rl = n ? min(warp_region_of(offsets, S, e - 1), S - 1) : S - 1;
-            if (lane == 0) {
-                sm.info[4] = rf;
-                sm.info[5] = rl;
-            }
+            sm.info[4] = min(region_of(offsets, 0, S + 1, b), S - 1);
+            sm.info[5] = n ? min(region_of(offsets, 0, S + 1, e - 1), S - 1) : S - 1;
+        }
+        __syncthreads();
+    }
+
+    // scan() for a tile whose regions the caller stored in info[4] and
+    // info[5] before the __syncthreads() that precedes it (from the scene's
+    // per-tile table): the prefix alone.  Ends with __syncthreads().
+    __device__ static __forceinline__ void scan_known_regions(Smem& sm)
+    {
+        if (threadIdx.x < 32) prefix_warp0(sm);
+        __syncthreads();
+    }
+
+    // Warp 0 alone, after the ballots are stored and a __syncthreads(): the
+    // same results as scan() (ballot-count prefix, total, the regions of
+    // the tile's first and last drawable), with no CTA barrier; warp 0 sees
+    // them after its own __syncwarp(), the other warps after the caller's
+    // next __syncthreads().  The whole warp finds each region in 32-way
+    // rounds (the lookback form's tiles need not be the scene table's).
+    __device__ static __forceinline__ void scan_warp0(Smem& sm, const uint32_t* __restrict__ offsets, uint32_t S,
+                                                      uint32_t b, uint32_t n)
+    {
+        const int lane = threadIdx.x & 31;
+        prefix_warp0(sm);
+        // Clamped to S-1 so that an empty scene (n == 0, one work item)
+        // stays inside the offsets and counts arrays.
+        const uint32_t e = min(b + (uint32_t)SIZE, n);
+        const uint32_t rf = min(warp_region_of(offsets, S, b), S - 1);
+        const uint32_t rl = n ? min(warp_region_of(offsets, S, e - 1), S - 1) : S - 1;
+        if (lane == 0) {
+            sm.info[4] = rf;
+            sm.info[5] = rl;
         }
         __syncwarp();
     }
@@ -267,6 +261,34 @@ struct Tile {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
         const uint32_t start_f = offsets[rf];
+        if (rf == rl) {
+            // The whole tile in one region: slot = base + the item's
+            // tile-local exclusive prefix (from its row's ballot and prefix).
+            const uint32_t lane = (uint32_t)t & 31u, warp = (uint32_t)t >> 5;
+            const uint32_t lt = (1u << lane) - 1u;
+            const uint32_t base = (start_f >= b) ? start_f - excl(sm, start_f - b) : start_f + carry;
+            const uint32_t dbase = kShard ? __ldg(sp.dst_base + rf) : 0u;
+#pragma unroll
+            for (int j = J0; j < J1; j++) {
+                if (!((vis_bits >> j) & 1u)) continue;
+                const uint32_t i = b + (uint32_t)(j * THREADS + t);
+                const uint32_t slot = base + sm.prefix[j * NW + warp] + __popc(sm.ballot[j][warp] & lt);
+                uint32_t out = slot;
+                if (kShard) out = (slot < n) ? dbase + (slot - start_f) : 0xffffffffu;
+                if (slot >= n || (kShard && out >= sp.capacity)) {
+                    atomicOr(error, CADR_DEVERR_BAD_INDEX);
+                    continue;
+                }
+                const uint4 e = ent[j - J0];
+                uint32_t* c = cmds + (size_t)out * 5;
+                c[0] = e.x;
+                c[1] = 1u;
+                c[2] = e.y;
+                c[3] = e.z;
+                c[4] = kShard ? i + sp.first_instance : i;
+            }
+            return;
+        }
 #pragma unroll
         for (int j = J0; j < J1; j++) {
             if (!((vis_bits >> j) & 1u)) continue;

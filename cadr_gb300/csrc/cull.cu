@@ -200,6 +200,9 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     const uint32_t tile = blockIdx.x, b = tile * (uint32_t)kLeafTile;
     const uint32_t stride = (uint32_t)leaf_plane_stride(a.n);
     const uint32_t* off = stage_offsets(s_off, a.off_cap, a.offsets, a.num_state_sets);
+    // The tile's first and last regions, from the scene's per-tile table,
+    // straight into info[4], info[5].
+    if (t == 0) cp_async_8(&sm.info[4], a.tile_region + tile);
     uint32_t vw[kLeafIpt], l0[kLeafIpt], l1[kLeafIpt], geo[kLeafIpt];
     {
         const uint4* pv = reinterpret_cast<const uint4*>(a.planes + tile * 64u + (uint32_t)warp * 8u);
@@ -227,9 +230,12 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     uint4 ent[kLeafIpt];
     LeafTile::gather(vis_bits, lod_bits, geo, a.lods, a.num_geometries, a.num_lods, a.error, ent);
     grid_dependency_wait();
-    if (t == 0) sm.info[2] = load_relaxed_u32(a.tile_words + tile);
+    if (t == 0) {
+        sm.info[2] = load_relaxed_u32(a.tile_words + tile);
+        cp_async_wait_all();
+    }
     __syncthreads();
-    LeafTile::scan(sm, off, a.num_state_sets, b, a.n);
+    LeafTile::scan_known_regions(sm);
     if (kShard)
         LeafTile::write_cmds<0, kLeafIpt, true>(sm, vis_bits, ent, b, a.n, off, a.cmds, a.error, a.shard);
     else

@@ -27,6 +27,7 @@ struct LeafArgs {
     const uint32_t* geometry;     // N
     const uint32_t* offsets;      // S + 1
     const uint32_t* tile_start;   // per leaf tile: start of the region holding its last drawable
+    const uint2* tile_region;     // per leaf tile: regions of its first and last drawable (clamped to S-1)
     uint32_t num_state_sets;
     const uint4* lods;            // G * L
     uint32_t num_geometries;
@@ -55,13 +56,14 @@ struct ViewJob {
     uint32_t* counts;
     uint32_t* marginal;
     const uint32_t* tile_start;   // the scene's per-tile region starts (tiles of kLeafTile drawables)
+    const uint2* tile_region;     // the scene's per-tile first and last regions (tiles of kLeafTile drawables)
     uint32_t n;
     uint32_t num_state_sets;
     uint32_t num_geometries;
     uint32_t num_lods;
     uint32_t first_item;          // first global work item of this view
     uint32_t num_tiles;
-    uint32_t pad[2];
+    uint32_t pad[4];
     ViewConst view;
 };
 

@@ -23,11 +23,12 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 static cadr_status before_upload(cadr_scene* sc);
 static cadr_status after_upload(cadr_scene* sc);
 
-// The plain pass's per-tile table: for each leaf tile of kLeafTile
+// The plain pass's per-tile tables: for each leaf tile of kLeafTile
 // drawables, the start of the StateSet region holding its last drawable
-// (the region search the stream kernel would otherwise do per CTA).  Built
-// on the host from the validated offsets at every commit, uploaded on the
-// upload stream.
+// (for the stream kernel) and the regions of its first and last drawable,
+// clamped to S-1 (for the write kernels): the region searches a CTA would
+// otherwise make.  Built on the host from the validated offsets at every
+// commit, uploaded on the upload stream.
 static cadr_status upload_tile_starts(cadr_scene* sc)
 {
     const uint64_t N = sc->desc.num_drawables;
@@ -35,16 +36,25 @@ static cadr_status upload_tile_starts(cadr_scene* sc)
     const std::vector<uint32_t>& off = sc->h_offsets;
     const uint64_t tiles = (N + kLeafTile - 1) / kLeafTile;
     sc->h_tile_start.resize(tiles);
+    sc->h_tile_region.resize(tiles * 2);
+    auto region = [&](uint32_t key) {
+        size_t r = (size_t)(std::upper_bound(off.begin(), off.end(), key) - off.begin()) - 1;
+        return (uint32_t)std::min<size_t>(r, S - 1);
+    };
     for (uint64_t t = 0; t < tiles; t++) {
+        const uint32_t first = (uint32_t)(t * kLeafTile);
         const uint32_t last = (uint32_t)(std::min<uint64_t>((t + 1) * kLeafTile, N) - 1);
-        size_t r = (size_t)(std::upper_bound(off.begin(), off.end(), last) - off.begin()) - 1;
-        if (r > S - 1) r = S - 1;
-        sc->h_tile_start[t] = off[r];
+        const uint32_t rl = region(last);
+        sc->h_tile_start[t] = off[rl];
+        sc->h_tile_region[2 * t] = region(first);
+        sc->h_tile_region[2 * t + 1] = rl;
     }
     if (tiles == 0) return CADR_OK;
     cadr_status st = before_upload(sc);
     if (st == CADR_OK)
         st = upload_bytes(sc->ctx, sc->tile_start, sc->h_tile_start.data(), tiles * 4, sc->ctx->upload_stream);
+    if (st == CADR_OK)
+        st = upload_bytes(sc->ctx, sc->tile_region, sc->h_tile_region.data(), tiles * 8, sc->ctx->upload_stream);
     if (st != CADR_OK) return st;
     return after_upload(sc);
 }
@@ -172,6 +182,7 @@ LeafArgs leaf_args(cadr_scene* sc)
     a.geometry = sc->buf.geometry;
     a.offsets = sc->buf.state_set_offsets;
     a.tile_start = sc->tile_start;
+    a.tile_region = reinterpret_cast<const uint2*>(sc->tile_region);
     a.num_state_sets = d.num_state_sets;
     a.lods = reinterpret_cast<const uint4*>(sc->buf.lods);
     a.num_geometries = d.num_geometries;
@@ -219,6 +230,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     const size_t o_world = off; off = align256(off + N * 64);
     const size_t o_wsph = off; off = align256(off + N * 16);
     const size_t o_tiles = off; off = align256(off + (N + kLeafTile - 1) / kLeafTile * 4);
+    const size_t o_treg = off; off = align256(off + (N + kLeafTile - 1) / kLeafTile * 8);
 
     auto* sc = new cadr_scene();
     sc->ctx = ctx;
@@ -246,6 +258,7 @@ CADR_API cadr_status cadr_scene_create(cadr_context* ctx, const cadr_scene_desc*
     sc->buf.world = reinterpret_cast<float*>(base + o_world);
     sc->buf.world_sphere = reinterpret_cast<float*>(base + o_wsph);
     sc->tile_start = reinterpret_cast<uint32_t*>(base + o_tiles);
+    sc->tile_region = reinterpret_cast<uint32_t*>(base + o_treg);
     // Defaults: all drawables in StateSet 0 until offsets are uploaded.
     std::vector<uint32_t> off0(d.num_state_sets + 1, (uint32_t)N);
     off0[0] = 0;
