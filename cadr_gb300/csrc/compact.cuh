@@ -376,8 +376,9 @@ __device__ __forceinline__ uint32_t leaf_tile_word(const uint32_t (*ballot)[kLea
 // carries: the visible drawables of the region holding the tile's first
 // drawable that precede the tile.  A segmented exclusive scan in chunks of
 // THREADS * PER tiles; a region start in a tile restarts the sum at that
-// tile's count, and the first tile's carry is 0.
-template <int THREADS, int PER>
+// tile's count, and the first tile's carry is 0.  With kVec (words + lo
+// 16-byte aligned) a thread's PER words move as 16-byte vectors.
+template <int THREADS, int PER, bool kVec = false>
 __device__ __forceinline__ void scan_tile_words(uint32_t* __restrict__ words, uint32_t lo, uint32_t hi)
 {
     __shared__ uint32_t s_val[THREADS / kWarp], s_head[THREADS / kWarp];
@@ -388,10 +389,20 @@ __device__ __forceinline__ void scan_tile_words(uint32_t* __restrict__ words, ui
     for (uint32_t c0 = lo; c0 < hi; c0 += (uint32_t)(THREADS * PER)) {
         uint32_t w[PER];
         uint32_t v = 0, h = 0;  // this thread's segmented total and whether it holds a head
+        const uint32_t i0 = c0 + (uint32_t)(t * PER);
+        const bool vec = kVec && (PER % 4 == 0) && i0 + PER <= hi;
+        if (vec) {
+#pragma unroll
+            for (int k = 0; k < PER; k += 4) {
+                const uint4 q = *reinterpret_cast<const uint4*>(words + i0 + k);
+                w[k] = q.x; w[k + 1] = q.y; w[k + 2] = q.z; w[k + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; k++) w[k] = i0 + k < hi ? words[i0 + k] : 0u;
+        }
 #pragma unroll
         for (int k = 0; k < PER; k++) {
-            const uint32_t idx = c0 + (uint32_t)(t * PER + k);
-            w[k] = idx < hi ? words[idx] : 0u;
             if (w[k] & kTileHead) {
                 v = w[k] & ~kTileHead;
                 h = 1;
@@ -441,11 +452,20 @@ __device__ __forceinline__ void scan_tile_words(uint32_t* __restrict__ words, ui
             if (lane > 0) ev = ph ? pv : ev + pv;
         }
         uint32_t run = ev;
+        uint32_t o[PER];
 #pragma unroll
         for (int k = 0; k < PER; k++) {
-            const uint32_t idx = c0 + (uint32_t)(t * PER + k);
-            if (idx < hi) words[idx] = run;
+            o[k] = run;
             run = (w[k] & kTileHead) ? (w[k] & ~kTileHead) : run + w[k];
+        }
+        if (vec) {
+#pragma unroll
+            for (int k = 0; k < PER; k += 4)
+                *reinterpret_cast<uint4*>(words + i0 + k) = make_uint4(o[k], o[k + 1], o[k + 2], o[k + 3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; k++)
+                if (i0 + k < hi) words[i0 + k] = o[k];
         }
         __syncthreads();
         if (t == THREADS - 1) s_run = run;

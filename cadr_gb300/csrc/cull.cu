@@ -177,7 +177,7 @@ constexpr int kScanPer = 8;
 __global__ void __launch_bounds__(kScanThreads) leaf_tile_scan_kernel(uint32_t* __restrict__ words, uint32_t tiles)
 {
     grid_dependents_launch();
-    scan_tile_words<kScanThreads, kScanPer>(words, 0u, tiles);
+    scan_tile_words<kScanThreads, kScanPer, true>(words, 0u, tiles);
 }
 
 
