@@ -12,21 +12,32 @@ namespace CadR {
 // ---------------------------------------------------------------------------
 // Backends.
 
+CudaMemoryBackend::~CudaMemoryBackend()
+{
+    if (_own && _ctx) cadr_context_destroy(_ctx);
+}
+
+cadr_context* CudaMemoryBackend::context() const
+{
+    if (!_ctx && _own) check(cadr_context_create(_device, &_ctx), "Renderer: context");
+    return _ctx;
+}
+
 uint64_t CudaMemoryBackend::allocBlock(size_t bytes)
 {
     void* p = nullptr;
-    if (cadr_device_alloc(_ctx, bytes, &p) != CADR_OK) return 0;
+    if (cadr_device_alloc(context(), bytes, &p) != CADR_OK) return 0;
     return reinterpret_cast<uint64_t>(p);
 }
 
 void CudaMemoryBackend::freeBlock(uint64_t address) noexcept
 {
-    cadr_device_free(_ctx, reinterpret_cast<void*>(address));
+    if (_ctx) cadr_device_free(_ctx, reinterpret_cast<void*>(address));
 }
 
 void CudaMemoryBackend::upload(uint64_t dst, const void* src, size_t bytes)
 {
-    check(cadr_upload(_ctx, reinterpret_cast<void*>(dst), src, bytes, nullptr), "DataStorage upload");
+    check(cadr_upload(context(), reinterpret_cast<void*>(dst), src, bytes, nullptr), "DataStorage upload");
 }
 
 void CudaMemoryBackend::flush() {}

@@ -3,6 +3,7 @@
 #include <CadR/Renderer.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <unordered_set>
 
@@ -59,6 +60,14 @@ void Drawable::destroy() noexcept
 // ---------------------------------------------------------------------------
 // StateSet (StateSet.cpp:20-47,180-268).
 
+// childList and parentList sit in a class that is not standard-layout;
+// offsetof is supported for it by the compilers this builds with.
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Winvalid-offsetof"
+const ParentChildListOffsets StateSet::parentChildListOffsets{offsetof(StateSet, parentList),
+                                                              offsetof(StateSet, childList)};
+#pragma GCC diagnostic pop
+
 StateSet::~StateSet()
 {
     for (Drawable* d : _drawables) d->_index = ~0u;
@@ -67,8 +76,11 @@ StateSet::~StateSet()
 
 void StateSet::removeChild(StateSet& child)
 {
-    auto it = std::find(childList.begin(), childList.end(), &child);
-    if (it != childList.end()) childList.erase(it);
+    for (auto it = childList.begin(); it != childList.end(); ++it)
+        if (&*it == &child) {
+            childList.remove(it);
+            return;
+        }
 }
 
 void StateSet::append(Drawable& d, const DrawableGpuData& g)
@@ -103,9 +115,9 @@ size_t StateSet::prepareRecording()
 {
     _skipRecording = !_forceRecording;
     size_t n = _records.size();
-    for (StateSet* c : childList) {
-        n += c->prepareRecording();
-        _skipRecording = _skipRecording && c->_skipRecording;
+    for (StateSet& c : childList) {
+        n += c.prepareRecording();
+        _skipRecording = _skipRecording && c._skipRecording;
     }
     _skipRecording = _skipRecording && n == 0;
     return n;
@@ -122,7 +134,7 @@ void StateSet::recordToCommandBuffer(std::vector<DrawCall>& out, size_t& counter
                                counter * sizeof(cadr_draw_indirect_cmd)});
         counter += n;
     }
-    for (StateSet* c : childList) c->recordToCommandBuffer(out, counter);
+    for (StateSet& c : childList) c.recordToCommandBuffer(out, counter);
 }
 
 void StateSet::recordDrawCalls(std::vector<DrawCall>& out, size_t& counter) const
@@ -135,7 +147,7 @@ void StateSet::recordDrawCalls(std::vector<DrawCall>& out, size_t& counter) cons
                                counter * sizeof(cadr_draw_indirect_cmd)});
         counter += n;
     }
-    for (const StateSet* c : childList) c->recordDrawCalls(out, counter);
+    for (const StateSet& c : childList) c.recordDrawCalls(out, counter);
 }
 
 // ---------------------------------------------------------------------------
@@ -143,8 +155,7 @@ void StateSet::recordDrawCalls(std::vector<DrawCall>& out, size_t& counter) cons
 
 Renderer::Renderer(int device)
 {
-    check(cadr_context_create(device, &_ownContext), "Renderer: context");
-    _ownBackend = std::make_unique<CudaMemoryBackend>(_ownContext);
+    _ownBackend = std::make_unique<CudaMemoryBackend>(device);
     _backend = _ownBackend.get();
     _storage = std::make_unique<DataStorage>(*_backend);
 }
@@ -156,14 +167,13 @@ Renderer::Renderer(MemoryBackend& backend) : _backend(&backend)
 
 Renderer::~Renderer()
 {
-    if (_ownContext) cadr_context_synchronize(_ownContext);
+    if (cadr_context* c = _backend->existingContext()) cadr_context_synchronize(c);
     if (_pack) cadr_pack_destroy(_pack);
     if (_drawables) _backend->freeBlock(_drawables);
     if (_indirect) _backend->freeBlock(_indirect);
     if (_pointers) _backend->freeBlock(_pointers);
     _storage.reset();
-    _ownBackend.reset();
-    if (_ownContext) cadr_context_destroy(_ownContext);
+    _ownBackend.reset();  // destroys the context this renderer created
 }
 
 size_t Renderer::beginFrame()
@@ -182,7 +192,7 @@ void Renderer::growBuffers(size_t n)
     if (_capacity >= n) return;
     size_t cap = size_t(float(n) * 1.2f);
     if (cap < 128) cap = 128;
-    if (_ownContext) cadr_context_synchronize(_ownContext);
+    if (cadr_context* c = _backend->existingContext()) cadr_context_synchronize(c);
     if (_drawables) _backend->freeBlock(_drawables);
     if (_indirect) _backend->freeBlock(_indirect);
     if (_pointers) _backend->freeBlock(_pointers);
@@ -295,9 +305,12 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
     // A StateSet reached twice (a child of two parents) is recorded twice,
     // which one slot per record cannot express: such a frame takes the
     // copying path.
+    // The walk also lists the tree's StateSets in a fixed order: when the
+    // list differs from the previous frame's (a child appended, removed or
+    // moved), the pack is laid out again.
     {
         std::unordered_set<const StateSet*> seen;
-        std::vector<const StateSet*> stack{&root};
+        std::vector<const StateSet*> stack{&root}, tree;
         while (!stack.empty()) {
             const StateSet* ss = stack.back();
             stack.pop_back();
@@ -305,7 +318,12 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
                 processDrawables(root, out, stream);
                 return;
             }
-            for (const StateSet* c : ss->childList) stack.push_back(c);
+            tree.push_back(ss);
+            for (const StateSet& c : ss->childList) stack.push_back(&c);
+        }
+        if (tree != _tree) {
+            _tree.swap(tree);
+            _layoutDirty = true;
         }
     }
     const size_t n = prepareSceneRendering(root);
@@ -329,7 +347,7 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
                 indexOf[ss->_slots[li]] = uint32_t(li);
             }
             id++;
-            for (auto it = ss->childList.rbegin(); it != ss->childList.rend(); ++it) stack.push_back(*it);
+            for (auto it = ss->childList.rbegin(); it != ss->childList.rend(); ++it) stack.push_back(&*it);
         }
         uint32_t rest = 0;
         for (uint32_t s = 0; s < slots; s++)

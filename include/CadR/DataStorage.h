@@ -38,21 +38,32 @@ public:
     virtual void upload(uint64_t dst, const void* src, size_t bytes) = 0;
     virtual void flush() {}                               // order uploads before the next pass
     virtual cadr_context* context() const { return nullptr; }
+    // The context if one exists already, without creating it.
+    virtual cadr_context* existingContext() const { return context(); }
 };
 
 // Device memory of a cadr_context; uploads staged through the context's
-// pinned ring on its upload stream.
+// pinned ring on its upload stream.  Either over the caller's context, or
+// over one of its own on CUDA device `device`, created at the first use
+// and destroyed with the backend.
 class CudaMemoryBackend : public MemoryBackend {
 public:
     explicit CudaMemoryBackend(cadr_context* ctx) : _ctx(ctx) {}
+    explicit CudaMemoryBackend(int device) : _device(device), _own(true) {}
+    ~CudaMemoryBackend() override;
+    CudaMemoryBackend(const CudaMemoryBackend&) = delete;
+    CudaMemoryBackend& operator=(const CudaMemoryBackend&) = delete;
     uint64_t allocBlock(size_t bytes) override;
     void freeBlock(uint64_t address) noexcept override;
     void upload(uint64_t dst, const void* src, size_t bytes) override;
     void flush() override;
-    cadr_context* context() const override { return _ctx; }
+    cadr_context* context() const override;
+    cadr_context* existingContext() const override { return _ctx; }
 
 private:
-    cadr_context* _ctx;
+    mutable cadr_context* _ctx = nullptr;
+    int _device = 0;
+    bool _own = false;
 };
 
 // Host memory standing in for device memory: one arena whose host addresses

@@ -8,9 +8,10 @@
 //                (src/CadR/MatrixList.h:54-59)
 //   Drawable     one DrawableGpuData record in its StateSet's list
 //                (src/CadR/Drawable.h:32-43, Drawable.cpp:35-78)
-//   StateSet     per-StateSet record list with O(1) swap-remove, child list,
-//                prepareRecording / recordToCommandBuffer in depth-first
-//                order (src/CadR/StateSet.cpp:20-47,180-268)
+//   StateSet     per-StateSet record list with O(1) swap-remove, child and
+//                parent lists (CadR/ParentChildList.h), prepareRecording /
+//                recordToCommandBuffer in depth-first order
+//                (src/CadR/StateSet.h:77-79, StateSet.cpp:20-47,180-268)
 //   Renderer     buffer growth x1.2 (min 128), drawable processing through
 //                cadr_process_drawables, uploads, frame timing
 //                (src/CadR/Renderer.cpp:446-720,946-999)
@@ -27,6 +28,7 @@
 #include <vector>
 
 #include "DataStorage.h"
+#include "ParentChildList.h"
 
 namespace CadR {
 
@@ -117,7 +119,10 @@ public:
     StateSet(const StateSet&) = delete;
     StateSet& operator=(const StateSet&) = delete;
 
-    void appendChild(StateSet& child) { childList.push_back(&child); }
+    Renderer& renderer() const { return *_renderer; }
+    bool forceRecording() const { return _forceRecording; }
+    void appendChild(StateSet& child) { childList.append(child); }
+    // Removes the first relation to `child`, if any.
     void removeChild(StateSet& child);
     size_t getNumDrawables() const { return _records.size(); }
     const std::vector<DrawableGpuData>& drawableDataList() const { return _records; }
@@ -129,7 +134,11 @@ public:
     // array is on the device: Renderer::processDrawablesResident).
     void recordDrawCalls(std::vector<DrawCall>& out, size_t& drawableCounter) const;
 
-    std::vector<StateSet*> childList;
+    // Where childList and parentList lie in a StateSet
+    // (src/CadR/StateSet.h:77-79).
+    static const ParentChildListOffsets parentChildListOffsets;
+    ChildList<StateSet, parentChildListOffsets> childList;
+    ParentList<StateSet, parentChildListOffsets> parentList;
 
 private:
     void append(Drawable& d, const DrawableGpuData& g);
@@ -153,7 +162,9 @@ struct FrameInfo {
 
 class Renderer {
 public:
-    // Renderer on CUDA device `device` (its own cadr_context).
+    // Renderer on CUDA device `device` with its own cadr_context, created at
+    // the first use of the device (so that the host side - StateSets,
+    // recording, handles - works on a machine without a GPU).
     explicit Renderer(int device = 0);
     // Renderer over a caller-provided backend; without a context only the
     // host side (allocation, handles, recording) is available.
@@ -201,11 +212,11 @@ private:
     std::vector<uint32_t> _freeSlots;
     std::vector<uint32_t> _newSlots;
     std::vector<DrawableGpuData> _newRecords;
+    std::vector<const StateSet*> _tree;  // the StateSets of the last resident frame, in walk order
     bool _layoutDirty = true;
     friend class StateSet;
     std::unique_ptr<MemoryBackend> _ownBackend;
     MemoryBackend* _backend;
-    cadr_context* _ownContext = nullptr;
     std::unique_ptr<DataStorage> _storage;
     size_t _frame = ~size_t(0);
     size_t _capacity = 0;

@@ -10,6 +10,9 @@
 //       does them;
 //     * StateSet depth-first packing, swap-remove and draw calls, with the
 //       oracle run over the host arena;
+//     * the StateSet child and parent lists: both sides linked by one
+//       append, unlinked by one remove, iteration both ways, destruction
+//       detaching an object from its parents and children;
 //   facade_test gpu   the CUDA Renderer: processDrawables on the device,
 //     compared word for word with the oracle over the downloaded blocks.
 // Exits 0 on success, prints the first failure otherwise.
@@ -390,6 +393,44 @@ static bool same_calls(const std::vector<DrawCall>& a, const std::vector<DrawCal
 // Device-resident recording against the copying path, frame by frame:
 // same draw calls, same buffers; new drawables and removals between frames;
 // a frame without changes launches nothing but processDrawables.
+// The child and parent lists (CadR/ParentChildList.h) over StateSets of a
+// renderer that never touches the device.
+static void test_parent_child_lists()
+{
+    Renderer r(0);
+    StateSet a(r), b(r), c(r);
+    EXPECT(a.childList.empty() && a.childList.size() == 0, "fresh child list not empty");
+    auto ab = a.childList.append(b);
+    a.childList.append(c);
+    EXPECT(a.childList.size() == 2 && &a.childList.front() == &b && &a.childList.back() == &c, "children of a");
+    EXPECT(b.parentList.size() == 1 && &b.parentList.front() == &a, "parent of b");
+    EXPECT(&*ab == &b && &ab->renderer() == &r, "iterator of the appended child");
+    std::vector<StateSet*> fwd, rev;
+    for (StateSet& x : a.childList) fwd.push_back(&x);
+    for (auto it = a.childList.rbegin(); it != a.childList.rend(); ++it) rev.push_back(&*it);
+    EXPECT(fwd == std::vector<StateSet*>({&b, &c}) && rev == std::vector<StateSet*>({&c, &b}), "iteration order");
+    // a parent appended from the child's side shows in the parent's children
+    c.parentList.append(b);
+    EXPECT(b.childList.size() == 1 && &b.childList.front() == &c && c.parentList.size() == 2 &&
+               &c.parentList.back() == &b, "append from the child's side");
+    a.childList.remove(ab);
+    EXPECT(a.childList.size() == 1 && b.parentList.empty(), "remove unlinks both sides");
+    {
+        StateSet d(r);
+        c.childList.append(d);
+        d.childList.append(a);
+        EXPECT(c.childList.size() == 1 && a.parentList.size() == 1, "links to d");
+    }
+    EXPECT(c.childList.empty() && a.parentList.empty(), "destroying d detaches it from its parent and child");
+    b.childList.clear();
+    EXPECT(b.childList.empty() && c.parentList.size() == 1 && &c.parentList.front() == &a, "clear");
+    const StateSet& ca = a;
+    size_t k = 0;
+    for (auto it = ca.childList.cbegin(); it != ca.childList.cend(); ++it) k++;
+    EXPECT(k == 1, "const iteration");
+    std::printf("parent/child lists ok\n");
+}
+
 static void test_gpu_resident()
 {
     Renderer r(0);
@@ -397,7 +438,7 @@ static void test_gpu_resident()
     r.beginFrame();
     build_scene(r, S, 120, 12000);
     cadr_context* ctx = r.context();
-    for (int frame = 0; frame < 3 && !g_fail; frame++) {
+    for (int frame = 0; frame < 5 && !g_fail; frame++) {
         if (frame == 1) {
             // Removals (swap-removes reorder the lists) and new drawables.
             for (size_t i = 3; i < S.drawables.size(); i += 11) S.drawables[i].destroy();
@@ -409,6 +450,11 @@ static void test_gpu_resident()
                 S.drawables.emplace_back(*S.geometries[i % S.geometries.size()], uint32_t(8 * (i % 3)), *ml, *sets[i % 3]);
                 S.lists.push_back(std::move(ml));
             }
+        }
+        if (frame == 3) {
+            // The tree alone changes: D moves from C to A.
+            S.c->removeChild(*S.d);
+            S.a->childList.append(*S.d);
         }
         std::vector<DrawCall> host, res;
         r.beginFrame();
@@ -425,10 +471,12 @@ static void test_gpu_resident()
         EXPECT(same_calls(host, res), "frame %d: draw calls differ", frame);
         EXPECT(std::memcmp(hi.data(), ri.data(), n * 16) == 0, "frame %d: indirect commands differ", frame);
         EXPECT(std::memcmp(hp.data(), rp.data(), n * 32) == 0, "frame %d: drawable pointers differ", frame);
-        if (frame == 2) EXPECT(launches == 1, "an unchanged frame launched %llu kernels", (unsigned long long)launches);
+        if (frame == 2 || frame == 4)
+            EXPECT(launches == 1, "an unchanged frame launched %llu kernels", (unsigned long long)launches);
+        if (frame == 3) EXPECT(launches > 1, "a tree change did not lay the pack out again");
         check(cadr_context_check_device_error(ctx, nullptr), "device error");
     }
-    std::printf("gpu resident: 3 frames equal to the copying path\n");
+    std::printf("gpu resident: 5 frames equal to the copying path\n");
 }
 
 int main(int argc, char** argv)
@@ -439,6 +487,7 @@ int main(int argc, char** argv)
             test_allocation_placement();
             if (!g_fail) test_handle_table();
             if (!g_fail) test_recording_and_oracle();
+            if (!g_fail) test_parent_child_lists();
         } else {
             test_gpu();
             if (!g_fail) test_gpu_resident();

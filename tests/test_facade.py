@@ -29,6 +29,7 @@ def test_facade_host_side(cuda_lib, oracle_lib, tmp_path):
     exe = _build(tmp_path)
     r = subprocess.run([str(exe), "cpu"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+    assert "parent/child lists ok" in r.stdout
     assert "facade cpu ok" in r.stdout
 
 
@@ -37,5 +38,24 @@ def test_facade_renderer_on_gpu(cuda_lib, oracle_lib, tmp_path):
     exe = _build(tmp_path)
     r = subprocess.run([str(exe), "gpu"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "gpu resident: 3 frames equal to the copying path" in r.stdout
+    assert "gpu resident: 5 frames equal to the copying path" in r.stdout
     assert "facade gpu ok" in r.stdout
+
+
+def test_reference_parent_child_test(cuda_lib):
+    """The reference's tests/ParentChildTest.cpp, compiled unchanged against
+    the facade's headers and library (oracle/Makefile, target ref-api), runs
+    to completion: StateSet's childList / parentList keep the reference's
+    interface.  Only where the CADR sources are present."""
+    from oracle import bind
+    from cadr_gb300 import build
+    ref = bind.reference_root()
+    if not ref:
+        pytest.skip("CADR sources not present")
+    build.build_facade()
+    oracle_dir = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-s", "--no-print-directory", "-C", oracle_dir, "ref-api", f"REF={ref}",
+                    f"LIB={os.path.dirname(build.FACADE_LIB)}"], check=True)
+    exe = os.path.join(oracle_dir, "_ref", "parent_child_test")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
