@@ -32,25 +32,54 @@ void MatrixList::setMatrices(const Mat4* m, size_t n)
 // ---------------------------------------------------------------------------
 // Drawable (Drawable.cpp:35-78).
 
-Drawable::Drawable(Geometry& g, uint32_t off, MatrixList& ml, StateSet& ss)
-{
-    ss.append(*this, DrawableGpuData{g.vertexDataAllocation().handle(), g.indexDataAllocation().handle(), ml.handle(),
-                                     0, g.primitiveSetDataAllocation().handle(), off, 0});
-}
+Drawable::Drawable(Geometry& g, uint32_t off, MatrixList& ml, StateSet& ss) { create(g, off, ml, nullptr, ss); }
 
 Drawable::Drawable(Geometry& g, uint32_t off, MatrixList& ml, DataAllocation& dd, StateSet& ss)
 {
-    ss.append(*this, DrawableGpuData{g.vertexDataAllocation().handle(), g.indexDataAllocation().handle(), ml.handle(),
-                                     dd.handle(), g.primitiveSetDataAllocation().handle(), off, 0});
+    create(g, off, ml, &dd, ss);
 }
 
-Drawable::Drawable(Drawable&& o) noexcept : _stateSet(o._stateSet), _index(o._index)
+void Drawable::create(Geometry& g, uint32_t off, MatrixList& ml, StateSet& ss) { create(g, off, ml, nullptr, ss); }
+
+void Drawable::create(Geometry& g, uint32_t off, MatrixList& ml, DataAllocation& dd, StateSet& ss)
+{
+    create(g, off, ml, &dd, ss);
+}
+
+// The record of Drawable.cpp:35-78: geometry handles, MatrixList handle,
+// drawable-data handle (0 without one), PrimitiveSet offset.
+void Drawable::create(Geometry& g, uint32_t off, MatrixList& ml, DataAllocation* dd, StateSet& ss)
+{
+    destroy();
+    _matrixList = &ml;
+    _drawableData = dd;
+    ss.append(*this, DrawableGpuData(g.vertexDataAllocation().handle(), g.indexDataAllocation().handle(), ml.handle(),
+                                     dd ? dd->handle() : 0, g.primitiveSetDataAllocation().handle(), off));
+}
+
+Drawable::Drawable(Drawable&& o) noexcept
+    : _stateSet(o._stateSet), _matrixList(o._matrixList), _drawableData(o._drawableData), _index(o._index)
 {
     if (_index != ~0u) _stateSet->_drawables[_index] = this;
     o._index = ~0u;
 }
 
+Drawable& Drawable::operator=(Drawable&& o) noexcept
+{
+    if (this == &o) return *this;
+    destroy();
+    _stateSet = o._stateSet;
+    _matrixList = o._matrixList;
+    _drawableData = o._drawableData;
+    _index = o._index;
+    if (_index != ~0u) _stateSet->_drawables[_index] = this;
+    o._index = ~0u;
+    return *this;
+}
+
 Drawable::~Drawable() { destroy(); }
+
+Renderer& Drawable::renderer() const { return _stateSet->renderer(); }
 
 void Drawable::destroy() noexcept
 {
@@ -68,10 +97,26 @@ const ParentChildListOffsets StateSet::parentChildListOffsets{offsetof(StateSet,
                                                               offsetof(StateSet, childList)};
 #pragma GCC diagnostic pop
 
-StateSet::~StateSet()
+StateSet::~StateSet() { removeAllDrawables(); }
+
+void StateSet::removeAllDrawables() noexcept
 {
     for (Drawable* d : _drawables) d->_index = ~0u;
     for (uint32_t s : _slots) _renderer->freeSlot(s);
+    _records.clear();
+    _drawables.clear();
+    _slots.clear();
+}
+
+void StateSet::appendDrawable(Drawable& d, const DrawableGpuData& g)
+{
+    if (d._index != ~0u) d._stateSet->remove(d);
+    append(d, g);
+}
+
+void StateSet::removeDrawable(Drawable& d) noexcept
+{
+    if (d._index != ~0u) d._stateSet->remove(d);
 }
 
 void StateSet::removeChild(StateSet& child)
@@ -114,6 +159,7 @@ void StateSet::remove(Drawable& d) noexcept
 size_t StateSet::prepareRecording()
 {
     _skipRecording = !_forceRecording;
+    for (auto& f : prepareCallList) f(*this);
     size_t n = _records.size();
     for (StateSet& c : childList) {
         n += c.prepareRecording();

@@ -22,8 +22,10 @@
 // the three steps in that order).  Matrices are column-major float[16].
 #pragma once
 
+#include <array>
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -48,6 +50,15 @@ struct DrawableGpuData {
     uint64_t primitiveSetHandle;
     uint32_t primitiveSetOffset;
     uint32_t padding;
+
+    DrawableGpuData() = default;
+    constexpr DrawableGpuData(uint64_t vertexData, uint64_t indexData, uint64_t matrixList, uint64_t drawableData,
+                              uint64_t primitiveSet, uint32_t primitiveSetOffset_)
+        : vertexDataHandle(vertexData), indexDataHandle(indexData), matrixListHandle(matrixList),
+          drawableDataHandle(drawableData), primitiveSetHandle(primitiveSet), primitiveSetOffset(primitiveSetOffset_),
+          padding(0)
+    {
+    }
 };
 static_assert(sizeof(DrawableGpuData) == 48, "DrawableGpuData must be 48 bytes (Drawable.cpp:13)");
 static_assert(sizeof(DrawableGpuData) == sizeof(cadr_drawable_gpu_data), "C ABI record");
@@ -90,13 +101,24 @@ public:
     Drawable(Drawable&& other) noexcept;
     Drawable(const Drawable&) = delete;
     Drawable& operator=(const Drawable&) = delete;
+    Drawable& operator=(Drawable&& rhs) noexcept;
     ~Drawable();
+    // (Re)creates the drawable in `ss`, leaving the StateSet it was in.
+    void create(Geometry& g, uint32_t primitiveSetOffset, MatrixList& ml, StateSet& ss);
+    void create(Geometry& g, uint32_t primitiveSetOffset, MatrixList& ml, DataAllocation& drawableData, StateSet& ss);
     void destroy() noexcept;
     bool isValid() const { return _index != ~0u; }
+    Renderer& renderer() const;
+    // The StateSet that draws it, or drew it last (after destroy()).
     StateSet& stateSet() const { return *_stateSet; }
+    MatrixList& matrixList() const { return *_matrixList; }
+    DataAllocation* drawableData() const { return _drawableData; }
 
 private:
+    void create(Geometry& g, uint32_t primitiveSetOffset, MatrixList& ml, DataAllocation* drawableData, StateSet& ss);
     StateSet* _stateSet = nullptr;
+    MatrixList* _matrixList = nullptr;
+    DataAllocation* _drawableData = nullptr;
     uint32_t _index = ~0u;
     friend class StateSet;
 };
@@ -121,12 +143,25 @@ public:
 
     Renderer& renderer() const { return *_renderer; }
     bool forceRecording() const { return _forceRecording; }
+    // Detaches every drawable (as the destructor does).
+    void destroy() noexcept { removeAllDrawables(); }
+    // Moves `d` here with record `g` (out of the StateSet it was in).
+    void appendDrawable(Drawable& d, const DrawableGpuData& g);
+    static void removeDrawable(Drawable& d) noexcept;
+    void removeAllDrawables() noexcept;
+    Drawable& getDrawable(size_t index) const { return *_drawables[index]; }
+    // From a prepareCallList function: record this StateSet in this frame
+    // even without drawables.
+    void requestRecording() { _skipRecording = false; }
     void appendChild(StateSet& child) { childList.append(child); }
     // Removes the first relation to `child`, if any.
     void removeChild(StateSet& child);
     size_t getNumDrawables() const { return _records.size(); }
     const std::vector<DrawableGpuData>& drawableDataList() const { return _records; }
     void setForceRecording(bool v) { _forceRecording = v; }
+
+    // Called at the start of prepareRecording(), before the children.
+    std::vector<std::function<void(StateSet&)>> prepareCallList;
 
     size_t prepareRecording();
     void recordToCommandBuffer(std::vector<DrawCall>& out, size_t& drawableCounter);

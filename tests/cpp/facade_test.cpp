@@ -13,6 +13,7 @@
 //     * the StateSet child and parent lists: both sides linked by one
 //       append, unlinked by one remove, iteration both ways, destruction
 //       detaching an object from its parents and children;
+//     * Drawable create / move / getters and StateSet's drawable functions;
 //   facade_test gpu   the CUDA Renderer: processDrawables on the device,
 //     compared word for word with the oracle over the downloaded blocks.
 // Exits 0 on success, prints the first failure otherwise.
@@ -431,6 +432,48 @@ static void test_parent_child_lists()
     std::printf("parent/child lists ok\n");
 }
 
+// Drawable and StateSet drawable functions: create / move / getters,
+// appendDrawable moving a drawable between StateSets, removeDrawable,
+// removeAllDrawables, prepareCallList.
+static void test_drawable_api()
+{
+    HostMemoryBackend be(16 << 20);
+    Renderer r(be);
+    Geometry g(r);
+    MatrixList ml(r);
+    ml.setMatrices(Mat4{});
+    DataAllocation dd(r.dataStorage());
+    dd.alloc(64);
+    StateSet s1(r), s2(r);
+    Drawable d1(g, 0, ml, s1), d2(g, 8, ml, dd, s1);
+    EXPECT(s1.getNumDrawables() == 2 && &s1.getDrawable(0) == &d1 && &s1.getDrawable(1) == &d2, "two drawables in s1");
+    EXPECT(&d2.matrixList() == &ml && d2.drawableData() == &dd && d1.drawableData() == nullptr && &d1.renderer() == &r,
+           "getters");
+    EXPECT(s1.drawableDataList()[1].drawableDataHandle == dd.handle() && s1.drawableDataList()[1].primitiveSetOffset == 8,
+           "record of d2");
+    s2.appendDrawable(d1, s1.drawableDataList()[0]);
+    EXPECT(s1.getNumDrawables() == 1 && &s1.getDrawable(0) == &d2 && s2.getNumDrawables() == 1 && &d1.stateSet() == &s2,
+           "appendDrawable moves d1 to s2");
+    Drawable d3;
+    d3 = std::move(d2);
+    EXPECT(!d2.isValid() && d3.isValid() && &s1.getDrawable(0) == &d3 && d3.drawableData() == &dd, "move assignment");
+    StateSet::removeDrawable(d3);
+    EXPECT(!d3.isValid() && s1.getNumDrawables() == 0 && &d3.stateSet() == &s1, "removeDrawable");
+    d3.create(g, 16, ml, s2);
+    EXPECT(s2.getNumDrawables() == 2 && s2.drawableDataList()[1].primitiveSetOffset == 16, "create");
+    s2.removeAllDrawables();
+    EXPECT(!d1.isValid() && !d3.isValid() && s2.getNumDrawables() == 0, "removeAllDrawables");
+    StateSet root(r), child(r);
+    root.appendChild(child);
+    int calls = 0;
+    child.prepareCallList.push_back([&calls](StateSet& s) {
+        calls++;
+        s.requestRecording();
+    });
+    EXPECT(root.prepareRecording() == 0 && calls == 1, "prepareCallList");
+    std::printf("drawable api ok\n");
+}
+
 static void test_gpu_resident()
 {
     Renderer r(0);
@@ -488,6 +531,7 @@ int main(int argc, char** argv)
             if (!g_fail) test_handle_table();
             if (!g_fail) test_recording_and_oracle();
             if (!g_fail) test_parent_child_lists();
+            if (!g_fail) test_drawable_api();
         } else {
             test_gpu();
             if (!g_fail) test_gpu_resident();

@@ -30,6 +30,7 @@ def test_facade_host_side(cuda_lib, oracle_lib, tmp_path):
     r = subprocess.run([str(exe), "cpu"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "parent/child lists ok" in r.stdout
+    assert "drawable api ok" in r.stdout
     assert "facade cpu ok" in r.stdout
 
 
