@@ -226,6 +226,9 @@ CADR_API cadr_status cadr_context_destroy(cadr_context* ctx)
     if (ctx->l2_fetch_set) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, ctx->prev_l2_fetch);
     scratch_release(ctx->scratch);
     scratch_release(ctx->shard_scratch);
+    for (int f = 0; f < cadr_context::kTsFrames; f++)
+        for (int k = 0; k < 4; k++)
+            if (ctx->ts_ev[f][k]) cudaEventDestroy(ctx->ts_ev[f][k]);
     for (int f = 0; f < cadr_context::kFrames; f++) {
         for (int k = 0; k < 4; k++)
             if (ctx->frame_ev[f][k]) cudaEventDestroy(ctx->frame_ev[f][k]);
@@ -330,6 +333,46 @@ CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_
         ctx->frame_tail++;
     }
     *num_frames = k;
+    return CADR_OK;
+}
+
+CADR_API cadr_status cadr_context_record_timestamp(cadr_context* ctx, uint64_t frame, uint32_t index,
+                                                  cadr_stream stream)
+{
+    if (!ctx || index > 3) return fail(CADR_ERR_INVALID_ARG, "record_timestamp: bad argument");
+    DeviceGuard dg(ctx->device);
+    const int f = (int)(frame % cadr_context::kTsFrames);
+    if (!ctx->ts_ev[f][index]) {
+        cudaError_t e = cudaEventCreate(&ctx->ts_ev[f][index]);
+        if (e != cudaSuccess) return cuda_fail(e, "record_timestamp: event");
+    }
+    if (ctx->ts_frame[f] != frame) {
+        ctx->ts_frame[f] = frame;
+        ctx->ts_mask[f] = 0;
+    }
+    cudaError_t e = cudaEventRecord(ctx->ts_ev[f][index], stream ? (cudaStream_t)stream : ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "record_timestamp: record");
+    ctx->ts_mask[f] |= 1u << index;
+    return CADR_OK;
+}
+
+CADR_API cadr_status cadr_context_read_timestamps(cadr_context* ctx, uint64_t frame, uint64_t* out_ns)
+{
+    if (!ctx || !out_ns) return fail(CADR_ERR_INVALID_ARG, "read_timestamps: null argument");
+    const int f = (int)(frame % cadr_context::kTsFrames);
+    if (ctx->ts_frame[f] != frame || ctx->ts_mask[f] != 0xFu)
+        return fail(CADR_ERR_INVALID_ARG, "read_timestamps: frame %llu does not have its four timestamps",
+                    (unsigned long long)frame);
+    DeviceGuard dg(ctx->device);
+    cudaError_t e = cudaEventSynchronize(ctx->ts_ev[f][3]);
+    if (e != cudaSuccess) return cuda_fail(e, "read_timestamps: wait");
+    out_ns[0] = 0;
+    for (int k = 1; k < 4; k++) {
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, ctx->ts_ev[f][0], ctx->ts_ev[f][k]);
+        if (e != cudaSuccess) return cuda_fail(e, "read_timestamps: elapsed");
+        out_ns[k] = (uint64_t)((double)ms * 1e6 + 0.5);
+    }
     return CADR_OK;
 }
 

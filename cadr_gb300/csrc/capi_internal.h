@@ -51,6 +51,12 @@ struct cadr_context {
     cudaEvent_t frame_ev[kFrames][4] = {};  // before levels, after levels, after stream kernel, after leaf stage
     cudaEvent_t level_ev[kFrames][CADR_MAX_LEVELS] = {};  // after level l's propagation (l >= 1)
     uint32_t frame_levels[kFrames] = {};
+    // Timestamps of the facade's frames (cadr_context_record_timestamp):
+    // four per frame, for the last kTsFrames frames.
+    static constexpr int kTsFrames = 4;
+    cudaEvent_t ts_ev[kTsFrames][4] = {};
+    uint64_t ts_frame[kTsFrames] = {~0ull, ~0ull, ~0ull, ~0ull};
+    uint32_t ts_mask[kTsFrames] = {};
     uint64_t frame_head = 0, frame_tail = 0;
 };
 

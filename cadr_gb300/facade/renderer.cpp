@@ -3,6 +3,7 @@
 #include <CadR/Renderer.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstddef>
 #include <cstring>
 #include <unordered_set>
@@ -226,10 +227,63 @@ size_t Renderer::beginFrame()
 {
     _frame++;
     _storage->setFrameNumber(_frame);
+    _currentInfo = FrameInfo{};
+    _currentInfo.frameNumber = _frame;
+    _currentInfo.cpuBeginFrame = getCpuTimestamp();
+    _currentInfo.gpuBeginFrame = _currentInfo.cpuBeginFrame;
+    _gpuStamps = 0;
     return _frame;
 }
 
-void Renderer::endFrame() {}
+uint64_t Renderer::getCpuTimestamp() const
+{
+    return uint64_t(std::chrono::duration_cast<std::chrono::nanoseconds>(
+                        std::chrono::steady_clock::now().time_since_epoch())
+                        .count());
+}
+
+void Renderer::setCollectFrameInfo(bool on, bool /*useCalibratedTimestamps*/) { _collect = on; }
+
+// GPU timestamp `index` of the current frame (FrameInfo's four GPU fields).
+void Renderer::timestamp(uint32_t index, cadr_stream stream)
+{
+    if (!_collect) return;
+    cadr_context* ctx = _backend->context();
+    if (!ctx) return;
+    if (index == 0) _currentInfo.gpuBeginExecution = getCpuTimestamp();
+    check(cadr_context_record_timestamp(ctx, _frame, index, stream), "Renderer: frame timestamp");
+    _gpuStamps |= 1u << index;
+    _frameStream = stream;
+}
+
+void Renderer::endFrame()
+{
+    _currentInfo.cpuEndFrame = getCpuTimestamp();
+    _endedHasGpu = false;
+    if (_collect && _gpuStamps == 7u) {
+        timestamp(3, _frameStream);
+        _endedHasGpu = true;
+        _endedGpuBase = _currentInfo.gpuBeginExecution;
+    }
+    _lastInfo = _currentInfo;
+    _endedFrame = _frame;
+}
+
+const FrameInfo& Renderer::getFrameInfo()
+{
+    if (_endedFrame == ~size_t(0) || !_endedHasGpu) {
+        _lastInfo.frameNumber = ~size_t(0);
+        return _lastInfo;
+    }
+    uint64_t ns[4];
+    check(cadr_context_read_timestamps(_backend->context(), _endedFrame, ns), "Renderer: frame timestamps");
+    _lastInfo.frameNumber = _endedFrame;
+    _lastInfo.gpuBeginExecution = _endedGpuBase + ns[0];
+    _lastInfo.gpuAfterTransfersAndBeforeDrawableProcessing = _endedGpuBase + ns[1];
+    _lastInfo.gpuAfterDrawableProcessingAndBeforeRendering = _endedGpuBase + ns[2];
+    _lastInfo.gpuEndExecution = _endedGpuBase + ns[3];
+    return _lastInfo;
+}
 
 // Buffer growth of Renderer::prepareSceneRendering (Renderer.cpp:461-592):
 // 20% extra, at least 128 drawables.
@@ -252,7 +306,9 @@ void Renderer::growBuffers(size_t n)
 
 size_t Renderer::prepareSceneRendering(StateSet& root)
 {
+    _currentInfo.cpuPrepareRecordingBegin = getCpuTimestamp();
     const size_t n = root.prepareRecording();
+    _currentInfo.cpuPrepareRecordingEnd = getCpuTimestamp();
     growBuffers(n);
     return n;
 }
@@ -260,7 +316,9 @@ size_t Renderer::prepareSceneRendering(StateSet& root)
 void Renderer::recordSceneRendering(StateSet& root, std::vector<DrawCall>& out)
 {
     size_t counter = 0;
+    _currentInfo.cpuRecordStateSetsBegin = getCpuTimestamp();
     root.recordToCommandBuffer(out, counter);
+    _currentInfo.cpuRecordStateSetsEnd = getCpuTimestamp();
 }
 
 size_t Renderer::executeCopyOperations() { return _storage->uploadPending(); }
@@ -271,19 +329,23 @@ void Renderer::recordDrawableProcessing(size_t n, cadr_stream stream)
     cadr_context* ctx = _backend->context();
     if (!ctx) throw LogicError("Renderer::recordDrawableProcessing(): this renderer has no CUDA context");
     if (n > _capacity) throw LogicError("Renderer::recordDrawableProcessing(): call prepareSceneRendering() first");
+    if (!(_gpuStamps & 1u)) timestamp(0, stream);
     check(cadr_upload(ctx, reinterpret_cast<void*>(_drawables), _staging.data(), n * sizeof(DrawableGpuData), stream),
           "Renderer: drawable upload");
+    timestamp(1, stream);
     check(cadr_process_drawables(ctx, _storage->handleLevel(), reinterpret_cast<const void*>(_storage->handleTableDeviceAddress()),
                                  reinterpret_cast<const cadr_drawable_gpu_data*>(_drawables), n,
                                  reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
                                  reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
           "Renderer: processDrawables");
+    timestamp(2, stream);
 }
 
 void Renderer::processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream)
 {
     const size_t n = prepareSceneRendering(root);
     recordSceneRendering(root, out);
+    if (n) timestamp(0, stream);
     executeCopyOperations();
     recordDrawableProcessing(n, stream);
 }
@@ -374,7 +436,10 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
     }
     const size_t n = prepareSceneRendering(root);
     size_t counter = 0;
+    _currentInfo.cpuRecordStateSetsBegin = getCpuTimestamp();
     root.recordDrawCalls(out, counter);
+    _currentInfo.cpuRecordStateSetsEnd = getCpuTimestamp();
+    if (n) timestamp(0, stream);
     executeCopyOperations();
     const uint32_t slots = uint32_t(_slotOwner.size());
     if (slots > _packCapacity) growPack(slots);
@@ -415,6 +480,7 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
     }
     _layoutDirty = false;
     if (n == 0) return;
+    timestamp(1, stream);
     // processDrawables straight from the pool (slots in creation order), so
     // no repack is needed; the first n packed positions are the drawn ones.
     check(cadr_pack_process_drawables(_pack, _storage->handleLevel(),
@@ -422,6 +488,7 @@ void Renderer::processDrawablesResident(StateSet& root, std::vector<DrawCall>& o
                                       reinterpret_cast<cadr_draw_indirect_cmd*>(_indirect),
                                       reinterpret_cast<cadr_drawable_pointers*>(_pointers), stream),
           "Renderer: processDrawables");
+    timestamp(2, stream);
 }
 
 }  // namespace CadR

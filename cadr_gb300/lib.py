@@ -119,6 +119,8 @@ _SIGS = {
     "cadr_debug_set_fault": ([vp, u32], i32),
     "cadr_context_set_collect_frame_info": ([vp, i32], i32),
     "cadr_context_get_frame_infos": ([vp, C.POINTER(FrameInfo), u32, C.POINTER(u32)], i32),
+    "cadr_context_record_timestamp": ([vp, u64, u32, vp], i32),
+    "cadr_context_read_timestamps": ([vp, u64, C.POINTER(u64)], i32),
     "cadr_device_alloc": ([vp, sz, C.POINTER(vp)], i32),
     "cadr_device_free": ([vp, vp], i32),
     "cadr_host_alloc_pinned": ([sz, C.POINTER(vp)], i32),

@@ -188,11 +188,27 @@ private:
     friend class Renderer;
 };
 
-// CadR::FrameInfo counterpart: GPU times of the last processed frame.
+// CadR::FrameInfo (src/CadR/FrameInfo.h:15-31), with the reference's
+// fields.  CPU timestamps are nanoseconds of the host's steady clock; GPU
+// timestamps are nanoseconds too (gpuTimestampPeriod() = 1e-9 s): the
+// frame's first GPU timestamp is the host clock when its first GPU work was
+// queued, and the others add the CUDA-event durations to it, so their
+// differences are exact GPU durations.  gpuBeginFrame equals cpuBeginFrame.
 struct FrameInfo {
     size_t frameNumber = ~size_t(0);
-    float uploadMs = 0;       // executeCopyOperations + record copy
-    float processingMs = 0;   // the drawable-processing kernel
+    uint64_t gpuBeginFrame = 0;
+    uint64_t cpuBeginFrame = 0;
+    uint64_t cpuPrepareRecordingBegin = 0;
+    uint64_t cpuPrepareRecordingEnd = 0;
+    uint64_t cpuRecordStateSetsBegin = 0;
+    uint64_t cpuRecordStateSetsEnd = 0;
+    std::vector<uint64_t> cpuUserTimestampList;
+    uint64_t cpuEndFrame = 0;
+    uint64_t gpuBeginExecution = 0;                             // before the frame's uploads
+    uint64_t gpuAfterTransfersAndBeforeDrawableProcessing = 0;  // after them
+    uint64_t gpuAfterDrawableProcessingAndBeforeRendering = 0;  // after the processDrawables kernel
+    uint64_t gpuEndExecution = 0;                               // at the frame's end (no rendering here)
+    static constexpr uint32_t gpuTimestampPoolSize = 4;
 };
 
 class Renderer {
@@ -214,6 +230,18 @@ public:
 
     size_t beginFrame();
     size_t prepareSceneRendering(StateSet& root);
+    // Frame timing (Renderer.h:155-163 of the reference).  While on, each
+    // frame with drawable processing records the four GPU timestamps of
+    // FrameInfo; getFrameInfo() returns the last frame ended by endFrame(),
+    // waiting for its GPU timestamps (frameNumber stays ~0 when the frame
+    // processed no drawables).  useCalibratedTimestamps has no effect.
+    bool collectFrameInfo() const { return _collect; }
+    void setCollectFrameInfo(bool on, bool useCalibratedTimestamps = false);
+    const FrameInfo& getFrameInfo();
+    const FrameInfo& getCurrentFrameInfo() const { return _currentInfo; }
+    double cpuTimestampPeriod() const { return 1e-9; }
+    float gpuTimestampPeriod() const { return 1e-9f; }
+    uint64_t getCpuTimestamp() const;
     void recordSceneRendering(StateSet& root, std::vector<DrawCall>& out);
     void recordDrawableProcessing(size_t numDrawables, cadr_stream stream = nullptr);
     void processDrawables(StateSet& root, std::vector<DrawCall>& out, cadr_stream stream = nullptr);
@@ -248,6 +276,14 @@ private:
     std::vector<uint32_t> _newSlots;
     std::vector<DrawableGpuData> _newRecords;
     std::vector<const StateSet*> _tree;  // the StateSets of the last resident frame, in walk order
+    void timestamp(uint32_t index, cadr_stream stream);
+    bool _collect = false;
+    FrameInfo _currentInfo, _lastInfo;
+    uint32_t _gpuStamps = 0;             // timestamps the current frame recorded
+    cadr_stream _frameStream = nullptr;  // the stream of the current frame's drawable processing
+    size_t _endedFrame = ~size_t(0);     // the frame getFrameInfo() reports
+    bool _endedHasGpu = false;
+    uint64_t _endedGpuBase = 0;
     bool _layoutDirty = true;
     friend class StateSet;
     std::unique_ptr<MemoryBackend> _ownBackend;

@@ -520,6 +520,19 @@ CADR_API cadr_status cadr_context_set_collect_frame_info(cadr_context* ctx, int 
 CADR_API cadr_status cadr_context_get_frame_infos(cadr_context* ctx, cadr_frame_info* out,
                                                   uint32_t max_frames, uint32_t* num_frames);
 
+/* GPU timestamps of the C++ facade's frames, for CadR::FrameInfo's four
+ * GPU fields (src/CadR/FrameInfo.h:26-29: begin of execution, after the
+ * transfers, after drawable processing, end of execution; written in
+ * Renderer.cpp:600-702).  record_timestamp records timestamp `index`
+ * (0..3) of frame `frame` on `stream` (null: the context's stream); the last
+ * 4 frames are kept.  read_timestamps waits for the frame's four timestamps
+ * and returns them in out_ns[4] as nanoseconds after timestamp 0
+ * (out_ns[0] = 0); CADR_ERR_INVALID_ARG when the frame has not recorded all
+ * four or was overwritten. */
+CADR_API cadr_status cadr_context_record_timestamp(cadr_context* ctx, uint64_t frame, uint32_t index,
+                                                  cadr_stream stream);
+CADR_API cadr_status cadr_context_read_timestamps(cadr_context* ctx, uint64_t frame, uint64_t* out_ns);
+
 /* Host-side check of the last pass's device error word (0 = no error). */
 CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t* error_bits);
 

@@ -14,8 +14,12 @@
 //       append, unlinked by one remove, iteration both ways, destruction
 //       detaching an object from its parents and children;
 //     * Drawable create / move / getters and StateSet's drawable functions;
+//     * FrameInfo's CPU timestamps;
 //   facade_test gpu   the CUDA Renderer: processDrawables on the device,
-//     compared word for word with the oracle over the downloaded blocks.
+//     compared word for word with the oracle over the downloaded blocks;
+//     the device-resident path frame by frame against the copying path
+//     (drawables and the StateSet tree changing between frames); FrameInfo's
+//     GPU timestamps.
 // Exits 0 on success, prints the first failure otherwise.
 #include <CadR/Renderer.h>
 
@@ -474,6 +478,73 @@ static void test_drawable_api()
     std::printf("drawable api ok\n");
 }
 
+// FrameInfo with the reference's fields: CPU timestamps in order on any
+// backend; on the GPU the four GPU timestamps of a frame with drawable
+// processing, in order, with a positive processing time.
+static void check_cpu_times(const FrameInfo& f, const char* where)
+{
+    EXPECT(f.cpuBeginFrame <= f.cpuPrepareRecordingBegin && f.cpuPrepareRecordingBegin <= f.cpuPrepareRecordingEnd &&
+               f.cpuPrepareRecordingEnd <= f.cpuRecordStateSetsBegin &&
+               f.cpuRecordStateSetsBegin <= f.cpuRecordStateSetsEnd && f.cpuRecordStateSetsEnd <= f.cpuEndFrame &&
+               f.gpuBeginFrame == f.cpuBeginFrame,
+           "%s: CPU timestamps out of order", where);
+}
+
+static void test_frame_info_host()
+{
+    HostMemoryBackend be(64 << 20);
+    Renderer r(be);
+    SceneBuild S;
+    r.setCollectFrameInfo(true);
+    r.beginFrame();
+    build_scene(r, S, 8, 100);
+    std::vector<DrawCall> calls;
+    r.prepareSceneRendering(*S.root);
+    r.recordSceneRendering(*S.root, calls);
+    r.endFrame();
+    const FrameInfo& f = r.getFrameInfo();
+    EXPECT(f.frameNumber == ~size_t(0), "a frame without GPU timestamps reported as valid");
+    check_cpu_times(f, "host frame");
+    EXPECT(r.cpuTimestampPeriod() == 1e-9 && r.gpuTimestampPeriod() == 1e-9f, "timestamp periods");
+    std::printf("frame info host ok\n");
+}
+
+static void test_gpu_frame_info()
+{
+    Renderer r(0);
+    SceneBuild S;
+    r.beginFrame();
+    build_scene(r, S, 64, 20000);
+    r.endFrame();
+    r.setCollectFrameInfo(true);
+    for (int k = 0; k < 3 && !g_fail; k++) {
+        std::vector<DrawCall> calls;
+        const size_t fn = r.beginFrame();
+        if (k == 2)
+            r.processDrawablesResident(*S.root, calls);
+        else
+            r.processDrawables(*S.root, calls);
+        r.endFrame();
+        const FrameInfo& f = r.getFrameInfo();
+        EXPECT(f.frameNumber == fn, "frame %d: frameNumber %zu, expected %zu", k, f.frameNumber, fn);
+        check_cpu_times(f, "gpu frame");
+        EXPECT(f.gpuBeginExecution <= f.gpuAfterTransfersAndBeforeDrawableProcessing &&
+                   f.gpuAfterTransfersAndBeforeDrawableProcessing < f.gpuAfterDrawableProcessingAndBeforeRendering &&
+                   f.gpuAfterDrawableProcessingAndBeforeRendering <= f.gpuEndExecution,
+               "frame %d: GPU timestamps out of order", k);
+        const double ms = double(f.gpuAfterDrawableProcessingAndBeforeRendering -
+                                 f.gpuAfterTransfersAndBeforeDrawableProcessing) * r.gpuTimestampPeriod() * 1e3;
+        EXPECT(ms > 0.0 && ms < 100.0, "frame %d: drawable processing %.4f ms", k, ms);
+    }
+    r.setCollectFrameInfo(false);
+    std::vector<DrawCall> calls;
+    r.beginFrame();
+    r.processDrawables(*S.root, calls);
+    r.endFrame();
+    EXPECT(r.getFrameInfo().frameNumber == ~size_t(0), "a frame without collection reported GPU timestamps");
+    std::printf("gpu frame info ok\n");
+}
+
 static void test_gpu_resident()
 {
     Renderer r(0);
@@ -532,9 +603,11 @@ int main(int argc, char** argv)
             if (!g_fail) test_recording_and_oracle();
             if (!g_fail) test_parent_child_lists();
             if (!g_fail) test_drawable_api();
+            if (!g_fail) test_frame_info_host();
         } else {
             test_gpu();
             if (!g_fail) test_gpu_resident();
+            if (!g_fail) test_gpu_frame_info();
         }
     } catch (const std::exception& e) {
         std::printf("FAIL: exception %s\n", e.what());

@@ -31,6 +31,7 @@ def test_facade_host_side(cuda_lib, oracle_lib, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "parent/child lists ok" in r.stdout
     assert "drawable api ok" in r.stdout
+    assert "frame info host ok" in r.stdout
     assert "facade cpu ok" in r.stdout
 
 
@@ -40,6 +41,7 @@ def test_facade_renderer_on_gpu(cuda_lib, oracle_lib, tmp_path):
     r = subprocess.run([str(exe), "gpu"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "gpu resident: 5 frames equal to the copying path" in r.stdout
+    assert "gpu frame info ok" in r.stdout
     assert "facade gpu ok" in r.stdout
 
 
