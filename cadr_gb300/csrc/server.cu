@@ -229,12 +229,21 @@ static void worker_main(cadr_server* srv)
         srv->cv.wait(lk, [&] { return srv->stop || !srv->pending.empty(); });
         if (srv->stop && srv->pending.empty()) break;
         // Batching window: from the oldest request's arrival, wait for more
-        // requests unless the batch is already full.
+        // requests, unless the batch is already full (views), the device is
+        // idle (no batch in flight: waiting only adds latency), or the
+        // pending work already fills the device (its resident tiles), as
+        // it then gains nothing from more requests.
         const uint64_t oldest = srv->pending.front()->submit_ns;
         uint32_t views = 0;
-        for (Request* r : srv->pending) views += r->num_views;
+        uint64_t items = 0;
+        for (Request* r : srv->pending) {
+            views += r->num_views;
+            items += (uint64_t)r->num_views * r->scene->desc.num_drawables;
+        }
+        const uint64_t fill = (uint64_t)srv->ctx->num_sms * srv->ctx->tuning.ctas_per_sm * batched_tile(srv->ctx->tuning);
         const uint64_t t = now_ns();
-        if (!srv->stop && views < srv->cfg.max_batch_views && t < oldest + srv->cfg.window_ns) {
+        if (!srv->stop && views < srv->cfg.max_batch_views && t < oldest + srv->cfg.window_ns && srv->inflight > 0 &&
+            items < fill) {
             srv->cv.wait_for(lk, std::chrono::nanoseconds(oldest + srv->cfg.window_ns - t));
             continue;
         }

@@ -553,7 +553,9 @@ CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault);
 typedef struct cadr_server_config {
     uint32_t max_inflight_batches; /* streams in rotation, >= 1 */
     uint32_t max_batch_views;      /* views per batch */
-    uint64_t window_ns;            /* batching window, e.g. 200000 */
+    uint64_t window_ns;            /* batching window, e.g. 200000: the longest a request waits for
+                                      others; none while no batch is in flight or once the pending
+                                      work fills the device */
     uint64_t memory_budget_bytes;  /* output memory the server may hold (0 = from free memory) */
     uint64_t reserve_bytes;        /* free device memory left untouched */
 } cadr_server_config;
