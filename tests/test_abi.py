@@ -94,3 +94,5 @@ def test_null_arguments_are_rejected(cuda_lib):
     assert cuda_lib.cadr_cull(None, None, None, None, None, None) == lib.INVALID_ARG
     assert cuda_lib.cadr_process_drawables(None, 1, None, None, 0, None, None, None) == lib.INVALID_ARG
     assert cuda_lib.cadr_server_submit(None, None, None, 0, None) == lib.INVALID_ARG
+    assert cuda_lib.cadr_context_record_timestamp(None, 0, 0, None) == lib.INVALID_ARG
+    assert cuda_lib.cadr_context_read_timestamps(None, 0, None) == lib.INVALID_ARG
