@@ -11,7 +11,7 @@
 namespace CadR {
 
 Geometry::Geometry(Renderer& r)
-    : _vertices(r.dataStorage()), _indices(r.dataStorage()), _primitiveSets(r.dataStorage())
+    : _renderer(&r), _vertices(r.dataStorage()), _indices(r.dataStorage()), _primitiveSets(r.dataStorage())
 {
 }
 
@@ -19,7 +19,7 @@ MatrixList::MatrixList(Renderer& r) : _list(r.dataStorage()) {}
 
 // Header {numMatrices, capacity, 7 x uint64 0} then the matrices
 // (MatrixList.h:54-58).
-void MatrixList::setMatrices(const Mat4* m, size_t n)
+void* MatrixList::newContent(size_t n)
 {
     StagingData s = _list.alloc(64 + 64 * n);
     uint8_t* p = s.data<uint8_t>();
@@ -27,7 +27,13 @@ void MatrixList::setMatrices(const Mat4* m, size_t n)
     const uint32_t n32 = uint32_t(n);
     std::memcpy(p, &n32, 4);
     std::memcpy(p + 4, &n32, 4);
-    if (n) std::memcpy(p + 64, m, 64 * n);
+    return p + 64;
+}
+
+void MatrixList::setMatrixData(const void* m, size_t n)
+{
+    void* p = newContent(n);
+    if (n) std::memcpy(p, m, 64 * n);
 }
 
 // ---------------------------------------------------------------------------

@@ -32,9 +32,22 @@
 #include "DataStorage.h"
 #include "ParentChildList.h"
 
+#if __has_include(<glm/mat4x4.hpp>) && !defined(CADR_FACADE_NO_GLM)
+#include <glm/mat4x4.hpp>
+#endif
+
 namespace CadR {
 
+// The matrix type of MatrixList: glm::mat4 where GLM is on the include
+// path (as in the reference, src/CadR/MatrixList.h:33-36), else 16 floats
+// in column-major order.  The library itself only moves 64-byte blocks, so
+// code built either way links against the same library.
+#if __has_include(<glm/mat4x4.hpp>) && !defined(CADR_FACADE_NO_GLM)
+using Mat4 = glm::mat4;
+#else
 using Mat4 = std::array<float, 16>;
+#endif
+static_assert(sizeof(Mat4) == 64, "a 4x4 float matrix");
 
 struct PrimitiveSet {
     uint32_t indexCount;
@@ -69,25 +82,57 @@ class StateSet;
 class Geometry {
 public:
     explicit Geometry(Renderer& r);
+    Geometry(Geometry&&) = default;
+    Geometry(const Geometry&) = delete;
+    Geometry& operator=(const Geometry&) = delete;
+    Renderer& renderer() const { return *_renderer; }
+    DataStorage& dataStorage() const { return _vertices.dataStorage(); }
+    size_t vertexDataSize() const { return _vertices.size(); }
+    size_t indexDataSize() const { return _indices.size(); }
+    size_t primitiveSetDataSize() const { return _primitiveSets.size(); }
+    DataAllocation& vertexDataAllocation() { return _vertices; }
+    const DataAllocation& vertexDataAllocation() const { return _vertices; }
+    DataAllocation& indexDataAllocation() { return _indices; }
+    const DataAllocation& indexDataAllocation() const { return _indices; }
+    DataAllocation& primitiveSetDataAllocation() { return _primitiveSets; }
+    const DataAllocation& primitiveSetDataAllocation() const { return _primitiveSets; }
     void uploadVertexData(const void* p, size_t n) { _vertices.upload(p, n); }
     void uploadIndexData(const void* p, size_t n) { _indices.upload(p, n); }
     void uploadPrimitiveSetData(const void* p, size_t n) { _primitiveSets.upload(p, n); }
-    DataAllocation& vertexDataAllocation() { return _vertices; }
-    DataAllocation& indexDataAllocation() { return _indices; }
-    DataAllocation& primitiveSetDataAllocation() { return _primitiveSets; }
+    StagingData createVertexStagingData(size_t n) { return _vertices.alloc(n); }
+    StagingData createIndexStagingData(size_t n) { return _indices.alloc(n); }
+    StagingData createPrimitiveSetStagingData(size_t n) { return _primitiveSets.alloc(n); }
+    void freeVertexData() { _vertices.free(); }
+    void freeIndexData() { _indices.free(); }
+    void freePrimitiveSetData() { _primitiveSets.free(); }
+    void freeData()
+    {
+        freeVertexData();
+        freeIndexData();
+        freePrimitiveSetData();
+    }
 
 private:
+    Renderer* _renderer;
     DataAllocation _vertices, _indices, _primitiveSets;
 };
 
 class MatrixList {
 public:
     explicit MatrixList(Renderer& r);
-    void setMatrices(const Mat4& m) { setMatrices(&m, 1); }
-    void setMatrices(const std::vector<Mat4>& m) { setMatrices(m.data(), m.size()); }
-    void setMatrices(const Mat4* m, size_t n);
+    MatrixList(MatrixList&&) = default;
+    void setMatrices(const Mat4& m) { setMatrixData(&m, 1); }
+    void setMatrices(const std::vector<Mat4>& m) { setMatrixData(m.data(), m.size()); }
+    void setMatrices(const Mat4* m, size_t n) { setMatrixData(m, n); }
+    // A new content of `n` matrices (header written), to be filled in place.
+    Mat4* editNewContent(size_t n) { return static_cast<Mat4*>(newContent(n)); }
     uint64_t handle() const { return _list.handle(); }
     uint64_t deviceAddress() const { return _list.deviceAddress(); }
+
+    // The 64-byte header {numMatrices, capacity, 0...} followed by n
+    // column-major 64-byte matrices (MatrixList.h:54-59).
+    void setMatrixData(const void* matrices, size_t n);
+    void* newContent(size_t n);
 
 private:
     DataAllocation _list;

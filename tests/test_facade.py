@@ -62,3 +62,25 @@ def test_reference_parent_child_test(cuda_lib):
     exe = os.path.join(oracle_dir, "_ref", "parent_child_test")
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_facade_with_glm(cuda_lib, tmp_path):
+    """With GLM on the include path the facade's matrix type is glm::mat4,
+    as in the reference: tests/cpp/facade_glm_test.cpp fills MatrixLists
+    from glm::mat4 values and in place (editNewContent) and uses the
+    Geometry helpers, against the same library.  GLM is the reference's
+    copy (3rdParty/GLM), so only where the CADR sources are present."""
+    from oracle import bind
+    from cadr_gb300 import build
+    ref = bind.reference_root()
+    if not ref:
+        pytest.skip("CADR sources (and their GLM) not present")
+    lib_dir = os.path.dirname(build.build_facade())
+    exe = tmp_path / "facade_glm_test"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.join(ref, "3rdParty", "GLM"),
+                    os.path.join(ROOT, "tests", "cpp", "facade_glm_test.cpp"), "-o", str(exe),
+                    "-L", lib_dir, "-lcadr", "-lcadr_cuda", f"-Wl,-rpath,{lib_dir}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "facade glm ok" in r.stdout
