@@ -206,20 +206,27 @@ void StateSet::recordDrawCalls(std::vector<DrawCall>& out, size_t& counter) cons
 // ---------------------------------------------------------------------------
 // Renderer.
 
-Renderer::Renderer(int device)
+Renderer* Renderer::_defaultRenderer = nullptr;
+
+Renderer::Renderer(bool makeDefault) : Renderer(0, makeDefault) {}
+
+Renderer::Renderer(int device, bool makeDefault)
 {
     _ownBackend = std::make_unique<CudaMemoryBackend>(device);
     _backend = _ownBackend.get();
     _storage = std::make_unique<DataStorage>(*_backend);
+    if (makeDefault) _defaultRenderer = this;
 }
 
-Renderer::Renderer(MemoryBackend& backend) : _backend(&backend)
+Renderer::Renderer(MemoryBackend& backend, bool makeDefault) : _backend(&backend)
 {
     _storage = std::make_unique<DataStorage>(*_backend);
+    if (makeDefault) _defaultRenderer = this;
 }
 
 Renderer::~Renderer()
 {
+    if (_defaultRenderer == this) _defaultRenderer = nullptr;
     if (cadr_context* c = _backend->existingContext()) cadr_context_synchronize(c);
     if (_pack) cadr_pack_destroy(_pack);
     if (_drawables) _backend->freeBlock(_drawables);

@@ -258,14 +258,19 @@ struct FrameInfo {
 
 class Renderer {
 public:
-    // Renderer on CUDA device `device` with its own cadr_context, created at
-    // the first use of the device (so that the host side - StateSets,
-    // recording, handles - works on a machine without a GPU).
-    explicit Renderer(int device = 0);
+    // Renderer on CUDA device 0 (or `device`) with its own cadr_context,
+    // created at the first use of the device (so that the host side -
+    // StateSets, recording, handles - works on a machine without a GPU).
+    // With makeDefault it becomes Renderer::get() (Renderer.cpp:64-73).
+    explicit Renderer(bool makeDefault = true);
+    explicit Renderer(int device, bool makeDefault = true);
     // Renderer over a caller-provided backend; without a context only the
     // host side (allocation, handles, recording) is available.
-    explicit Renderer(MemoryBackend& backend);
+    explicit Renderer(MemoryBackend& backend, bool makeDefault = true);
     ~Renderer();
+    // The default renderer (Renderer.h:109-110, 220-221).
+    static Renderer& get() { return *_defaultRenderer; }
+    static void set(Renderer& r) noexcept { _defaultRenderer = &r; }
     Renderer(const Renderer&) = delete;
     Renderer& operator=(const Renderer&) = delete;
 
@@ -331,6 +336,7 @@ private:
     uint64_t _endedGpuBase = 0;
     bool _layoutDirty = true;
     friend class StateSet;
+    static Renderer* _defaultRenderer;
     std::unique_ptr<MemoryBackend> _ownBackend;
     MemoryBackend* _backend;
     std::unique_ptr<DataStorage> _storage;

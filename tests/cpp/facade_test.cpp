@@ -475,6 +475,14 @@ static void test_drawable_api()
         s.requestRecording();
     });
     EXPECT(root.prepareRecording() == 0 && calls == 1, "prepareCallList");
+    EXPECT(&Renderer::get() == &r, "the last renderer made default");
+    {
+        Renderer other(be, false);
+        EXPECT(&Renderer::get() == &r, "makeDefault false leaves the default");
+        Renderer::set(other);
+        EXPECT(&Renderer::get() == &other, "Renderer::set");
+    }
+    Renderer::set(r);
     std::printf("drawable api ok\n");
 }
 
