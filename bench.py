@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of request stream")
     ap.add_argument("--serving-scenes", type=int, default=64)
-    ap.add_argument("--inflight", type=int, default=4, help="serving: batches in flight")
+    ap.add_argument("--inflight", type=int, default=8, help="serving: batches in flight")
     return ap.parse_args()
 
 
@@ -591,7 +591,7 @@ def run_pack(ctx, im, steps: int, warmup: int, peak: float, tier_a_ms: float, re
 
 
 def measure_serving(ctx, rate: float, duration: float, plain_duration: float, num_scenes: int = 64,
-                    inflight: int = 4) -> dict:
+                    inflight: int = 8) -> dict:
     """Serving form on C5: 64 resident scenes (10,000 .. 8,000,000 drawables,
     log-uniform, built as C2 with seeds 4000+i), a Poisson stream of cull
     requests (`rate` per second for `duration` seconds, 1-4 views each,
