@@ -72,9 +72,11 @@ constexpr int kLeafIpt = 8;
 constexpr int kLeafTile = kLeafThreads * kLeafIpt;
 constexpr int kLeafWarps = kLeafThreads / 32;
 // Write kernels: StateSet offsets staged in shared memory up to this many
-// entries; 40 registers give 6 CTAs per SM (5 and 8 measured slower).
+// entries.  48 registers give 5 CTAs per SM without spills: the 40 that 6
+// CTAs allow spill 12-36 bytes a thread and measured 1% slower on the deep
+// hierarchy; 4 CTAs (56 registers) measured slower on the plain pass.
 constexpr uint32_t kWriteOffsetCap = 4096;
-constexpr int kWriteCtasPerSm = 6;
+constexpr int kWriteCtasPerSm = 5;
 constexpr int kPropThreads = 256;
 
 // Internal level: world[i] = parent_world[parent[i]] * local[i].
