@@ -53,3 +53,20 @@ def test_misaligned_and_empty(ctx):
     assert ctx.lib.cadr_process_drawables(ctx.handle, 1, buf.ptr, buf.ptr + 8, 4, buf.ptr, buf.ptr, None) == lib.INVALID_ARG
     assert ctx.lib.cadr_process_drawables(ctx.handle, 4, buf.ptr, buf.ptr, 4, buf.ptr, buf.ptr, None) == lib.INVALID_ARG
     assert ctx.lib.cadr_process_drawables(ctx.handle, 2, buf.ptr, buf.ptr, 0, buf.ptr, buf.ptr, None) == lib.OK
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n=1),
+    dict(n=33, num_geometries=5),
+    dict(n=32767, matrices_per_list=3),
+    dict(n=32769, with_drawable_data=False),
+    dict(n=70001, num_geometries=7, prims_per_geometry=5),
+])
+def test_ragged_sizes_against_oracle(ctx, kw):
+    """Counts that end inside a warp, a CTA or one past the shader's
+    32,768-workgroup dispatch row; MatrixLists of several matrices, no
+    drawable data (handle 0) and uneven PrimitiveSet counts."""
+    im, g_ind, g_ptr, r_ind, r_ptr = run_tier_a(ctx, kw, seed=11)
+    assert g_ind.shape[0] == kw["n"]
+    assert np.array_equal(g_ind, r_ind)
+    assert np.array_equal(g_ptr, r_ptr)

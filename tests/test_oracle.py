@@ -234,6 +234,7 @@ def test_tier_a_reference_shader_known_answers(oracle_lib, level):
     dict(n=2500, with_drawable_data=False),
     dict(n=1200, num_geometries=40, geometry_data=True),
     dict(n=900, num_geometries=30, extra_handles=2048 * 2048),
+    dict(n=32769, num_geometries=7, prims_per_geometry=5),  # a second dispatch row
 ])
 def test_tier_a_oracle_matches_reference_shader(oracle_lib, kw):
     """The oracle against the reference shader on images of each handle-table
