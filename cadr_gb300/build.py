@@ -73,6 +73,40 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     return LIB
 
 
+CHECKED_DIR = os.path.join(OUT_DIR, "checked")
+CHECKED_LIB = os.path.join(OUT_DIR, "libcadr_cuda_checked.so")
+
+
+def build_checked(force: bool = False) -> str:
+    """The bounds-checked build of the same sources (CADR_BOUNDS_CHECK
+    defined): every index a kernel derives itself is checked before the
+    access it guards, a failed check sets CADR_DEVERR_BOUNDS and skips the
+    access.  For tests on small cases; it is not the product library."""
+    os.makedirs(CHECKED_DIR, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(ROOT, "include", "cadr_cuda.h"))
+    srcs = sources()
+    objs = [os.path.join(CHECKED_DIR, os.path.basename(s)[:-3] + ".o") for s in srcs]
+
+    def compile_one(pair):
+        src, obj = pair
+        if not force and not _stale(obj, [src] + headers):
+            return
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-DCADR_BOUNDS_CHECK", "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        list(ex.map(compile_one, zip(srcs, objs)))
+    if force or _stale(CHECKED_LIB, objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", CHECKED_LIB, *objs, "-lcudart", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return CHECKED_LIB
+
+
 FACADE_DIR = os.path.join(HERE, "facade")
 FACADE_LIB = os.path.join(OUT_DIR, "libcadr.so")
 

@@ -124,6 +124,12 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batched_kernel(const 
         typename T::Smem& S = sm[cur];
         const uint32_t n = job.n;
         const uint32_t b = (item - job.first_item) * (uint32_t)T::SIZE;
+        // The warp search found the item's job: the item is one of its
+        // tiles.  (Reads are clamped and writes check their regions; this
+        // reports a wrong job table.)
+        if (t == 0)
+            (void)CADR_CHECKED(item >= job.first_item && item - job.first_item < max(1u, (n + T::SIZE - 1) / T::SIZE),
+                               error);
         uint32_t vis_bits = 0, lod_bits = 0;
         uint32_t geo[IPT];
         float4 wsv[IPT];
@@ -275,6 +281,7 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) batched_write_k
     const uint32_t n = J->n, S = J->num_state_sets;
     const uint32_t tile = item - J->first_item;
     const uint32_t b = tile * (uint32_t)kLeafTile;
+    if (t == 0) (void)CADR_CHECKED(item >= J->first_item && tile < max(1u, J->num_tiles), error);
     const uint32_t* off = stage_offsets(s_off, kWriteOffsetCap, J->offsets, S);
     if (t == 0 && n) cp_async_8(&sm.info[4], J->tile_region + tile);
     const uint32_t* geometry = J->geometry;

@@ -293,6 +293,31 @@ __device__ __forceinline__ void classify(const ViewConst& v, const float4 ws, ui
     lod = l;
 }
 
+// Internal-consistency checks.  In the bounds-checked build (CADR_BOUNDS_CHECK
+// defined) CADR_CHECKED(cond, error) evaluates cond, records
+// CADR_DEVERR_BOUNDS in *error when it is false and returns it, so that the
+// access it guards is skipped; in the product build it is the constant true
+// and cond is not evaluated.  It guards indices that the kernels derive
+// themselves (slots, plane words, work items); indices read from the
+// caller's data are checked in every build (CADR_DEVERR_BAD_INDEX).
+#ifdef CADR_BOUNDS_CHECK
+__device__ __forceinline__ bool bounds_checked(bool ok, uint32_t* error)
+{
+    if (!ok) atomicOr(error, CADR_DEVERR_BOUNDS);
+    return ok;
+}
+#define CADR_CHECKED(cond, error) (::cadr::bounds_checked((cond), (error)))
+#else
+#define CADR_CHECKED(cond, error) true
+#endif
+
+// Whether position i and its command slot both lie in region r.
+__device__ __forceinline__ bool in_region(const uint32_t* offsets, uint32_t r, uint32_t i, uint32_t slot)
+{
+    const uint32_t s = offsets[r], e = offsets[r + 1];
+    return s <= i && i < e && s <= slot && slot < e;
+}
+
 // First index s in [lo, hi) with offsets[s] > key, minus one: the region
 // that contains position `key` (regions may be empty).  `offsets` may point
 // to global or (staged) shared memory.

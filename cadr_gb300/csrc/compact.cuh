@@ -244,7 +244,7 @@ struct Tile {
                                                      uint32_t* error)
     {
         write_cmds<0, IPT>(sm, vis_bits, ent, b, n, offsets, cmds, error);
-        write_counts(sm, b, n, first_tile, offsets, S, counts);
+        write_counts(sm, b, n, first_tile, offsets, S, counts, error);
     }
 
     // The commands of the thread's visible items in rows [J0, J1); bit j of
@@ -279,6 +279,7 @@ struct Tile {
                     atomicOr(error, CADR_DEVERR_BAD_INDEX);
                     continue;
                 }
+                if (!CADR_CHECKED(in_region(offsets, rf, i, slot), error)) continue;
                 const uint4 e = ent[j - J0];
                 uint32_t* c = cmds + (size_t)out * 5;
                 c[0] = e.x;
@@ -303,6 +304,7 @@ struct Tile {
                 atomicOr(error, CADR_DEVERR_BAD_INDEX);
                 continue;
             }
+            if (!CADR_CHECKED(in_region(offsets, r, i, slot), error)) continue;
             const uint4 e = ent[j - J0];
             uint32_t* c = cmds + (size_t)out * 5;
             c[0] = e.x;
@@ -317,7 +319,7 @@ struct Tile {
     // scan's first tile also writes the zero counts of empty regions).
     __device__ static __forceinline__ void write_counts(const Smem& sm, uint32_t b, uint32_t n, bool first_tile,
                                                         const uint32_t* __restrict__ offsets, uint32_t S,
-                                                        uint32_t* __restrict__ counts)
+                                                        uint32_t* __restrict__ counts, uint32_t* error)
     {
         const int t = threadIdx.x;
         const uint32_t carry = sm.info[2], rf = sm.info[4], rl = sm.info[5];
@@ -326,7 +328,8 @@ struct Tile {
             const uint32_t sk = offsets[k], ek = offsets[k + 1];
             if (ek > sk && ek > b && ek <= e_tile) {
                 const uint32_t ee = excl(sm, ek - b);
-                counts[k] = (sk >= b) ? ee - excl(sm, sk - b) : carry + ee;
+                const uint32_t c = (sk >= b) ? ee - excl(sm, sk - b) : carry + ee;
+                if (CADR_CHECKED(c <= ek - sk, error)) counts[k] = c;
             }
         }
         if (first_tile)

@@ -128,10 +128,12 @@ __device__ __forceinline__ void stream_tile(const LeafArgs& a, uint32_t b, uint3
                 if (i0 < a.n) {
                     const uint32_t w = i0 >> 5;
                     const uint32_t wt = (i0 >> 11) * 64u + (uint32_t)warp * 8u + (uint32_t)j;
-                    a.planes[wt] = vb;
-                    a.planes[words + wt] = lb0;
-                    a.planes[2 * words + wt] = lb1;
-                    if (a.marginal) a.marginal[w] = mb;
+                    if (CADR_CHECKED(wt < words, a.error)) {
+                        a.planes[wt] = vb;
+                        a.planes[words + wt] = lb0;
+                        a.planes[2 * words + wt] = lb1;
+                    }
+                    if (a.marginal && CADR_CHECKED(w < (a.n + 31u) / 32u, a.error)) a.marginal[w] = mb;
                 }
             }
         }
@@ -233,6 +235,13 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     if (t == 0) {
         sm.info[2] = load_relaxed_u32(a.tile_words + tile);
         cp_async_wait_all();
+        // The scene's table against the offsets: the tile's first and last
+        // drawables lie in its first and last regions.  (The command writes
+        // check their own regions; this only reports a stale table.)
+        const uint32_t rf = sm.info[4], rl = sm.info[5], e = min(b + (uint32_t)kLeafTile, a.n) - 1u;
+        (void)CADR_CHECKED(rf <= rl && rl < a.num_state_sets && in_region(a.offsets, rf, b, b) &&
+                               in_region(a.offsets, rl, e, e),
+                           a.error);
     }
     __syncthreads();
     LeafTile::scan_known_regions(sm);

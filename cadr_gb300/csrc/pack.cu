@@ -154,6 +154,10 @@ __global__ void pack_place_kernel(const uint32_t* __restrict__ set_of_slot, cons
         return;
     }
     const uint32_t p = start[s] + li;
+    if (!CADR_CHECKED(p < n, error)) {
+        pos_of_slot[k] = kNoSlot;
+        return;
+    }
     pos_of_slot[k] = p;
     if (atomicExch(&slot_of_pos[p], k) != kNoSlot) atomicOr(error, CADR_DEVERR_BAD_INDEX);
 }

@@ -14,13 +14,15 @@ from .scenes import CMD_DTYPE, LOD_DTYPE, Scene
 from .views import VIEW_DTYPE
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libcadr_cuda.so")
+# CADR_CUDA_LIB names another build of the same C ABI to load instead (the
+# bounds-checked build, cadr_gb300.build.build_checked(), in its tests).
+LIB_PATH = os.environ.get("CADR_CUDA_LIB") or os.path.join(HERE, "_lib", "libcadr_cuda.so")
 MAX_LEVELS = 16
 
 STATUS = {0: "CADR_OK", 1: "CADR_ERR_INVALID_ARG", 2: "CADR_ERR_OUT_OF_MEMORY", 3: "CADR_ERR_TIMEOUT",
           4: "CADR_ERR_CUDA", 5: "CADR_ERR_DEVICE", 6: "CADR_ERR_NOT_READY", 7: "CADR_ERR_REJECTED"}
 OK, INVALID_ARG, OUT_OF_MEMORY, TIMEOUT, CUDA, DEVICE, NOT_READY, REJECTED = range(8)
-DEVERR_LOOKBACK_TIMEOUT, DEVERR_MBARRIER_TIMEOUT, DEVERR_BAD_INDEX = 0x1, 0x2, 0x4
+DEVERR_LOOKBACK_TIMEOUT, DEVERR_MBARRIER_TIMEOUT, DEVERR_BAD_INDEX, DEVERR_BOUNDS = 0x1, 0x2, 0x4, 0x8
 FAULT_NONE, FAULT_SKIP_FIRST_TILE_PUBLISH = 0, 1
 
 # Exported symbols of the C ABI (checked against include/cadr_cuda.h by the tests).

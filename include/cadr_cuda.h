@@ -57,6 +57,12 @@ typedef enum cadr_status {
 #define CADR_DEVERR_LOOKBACK_TIMEOUT 0x1u
 #define CADR_DEVERR_MBARRIER_TIMEOUT 0x2u
 #define CADR_DEVERR_BAD_INDEX 0x4u
+/* Set only by the bounds-checked build of this library (its sources
+ * compiled with CADR_BOUNDS_CHECK defined): an index derived inside a
+ * kernel (a command slot outside its StateSet region, a plane word past
+ * its plane, a work item outside its job) left its range, and the access
+ * it guarded was skipped. */
+#define CADR_DEVERR_BOUNDS 0x8u
 
 typedef void* cadr_stream; /* cudaStream_t */
 typedef struct cadr_context cadr_context;
