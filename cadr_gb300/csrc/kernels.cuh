@@ -72,9 +72,11 @@ constexpr int kLeafIpt = 8;
 constexpr int kLeafTile = kLeafThreads * kLeafIpt;
 constexpr int kLeafWarps = kLeafThreads / 32;
 // Write kernels: StateSet offsets staged in shared memory up to this many
-// entries.  48 registers give 5 CTAs per SM without spills: the 40 that 6
-// CTAs allow spill 12-36 bytes a thread and measured 1% slower on the deep
-// hierarchy; 4 CTAs (56 registers) measured slower on the plain pass.
+// entries.  48 registers give 5 CTAs per SM (the plain instance spills 8
+// bytes a thread there, the shard instance nothing); the 40 that 6 CTAs
+// allow spill 12 and 28 bytes and measured 1% slower on the deep
+// hierarchy; 4 CTAs (56 registers, no spills) measured slower on the plain
+// pass.
 constexpr uint32_t kWriteOffsetCap = 4096;
 constexpr int kWriteCtasPerSm = 5;
 constexpr int kPropThreads = 256;
