@@ -152,6 +152,15 @@ extern "C" {
 
 CADR_API int cadr_abi_version(void) { return 1; }
 
+CADR_API uint32_t cadr_build_flags(void)
+{
+#ifdef CADR_BOUNDS_CHECK
+    return CADR_BUILD_BOUNDS_CHECK;
+#else
+    return 0u;
+#endif
+}
+
 CADR_API const char* cadr_status_string(cadr_status s)
 {
     switch (s) {

@@ -103,6 +103,7 @@ _SIGS = {
     "cadr_status_string": ([i32], C.c_char_p),
     "cadr_last_error": ([], C.c_char_p),
     "cadr_abi_version": ([], i32),
+    "cadr_build_flags": ([], u32),
     "cadr_context_create": ([i32, C.POINTER(vp)], i32),
     "cadr_context_destroy": ([vp], i32),
     "cadr_context_stream": ([vp], vp),

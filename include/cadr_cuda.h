@@ -170,6 +170,11 @@ typedef struct cadr_scene_buffers {
 CADR_API const char* cadr_status_string(cadr_status s);
 CADR_API const char* cadr_last_error(void);
 CADR_API int cadr_abi_version(void);
+/* How this library was built: CADR_BUILD_BOUNDS_CHECK when its kernels
+ * check the indices they derive (the test build; see CADR_DEVERR_BOUNDS),
+ * 0 for the product build. */
+#define CADR_BUILD_BOUNDS_CHECK 0x1u
+CADR_API uint32_t cadr_build_flags(void);
 
 /* Creates the per-device context: streams (compute + upload), pinned staging
  * ring and lookback scratch.  Replaces the Vulkan device/queue the reference

@@ -76,6 +76,7 @@ def test_status_strings_and_no_device_error(cuda_lib):
     from cadr_gb300 import lib
     assert cuda_lib.cadr_status_string(lib.TIMEOUT) == b"timeout"
     assert cuda_lib.cadr_abi_version() == 1
+    assert cuda_lib.cadr_build_flags() == 0  # the product build
     try:
         import torch
         has_gpu = torch.cuda.is_available()

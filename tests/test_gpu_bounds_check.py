@@ -22,6 +22,9 @@ def test_parity_suite_under_the_bounds_checked_build(cuda_lib):
     from cadr_gb300 import build
     path = build.build_checked()
     env = dict(os.environ, CADR_CUDA_LIB=path)
+    probe = subprocess.run([sys.executable, "-c", "from cadr_gb300 import lib; print(lib.load().cadr_build_flags())"],
+                           env=env, cwd=ROOT, capture_output=True, text=True, timeout=120)
+    assert probe.stdout.strip() == "1", probe.stdout + probe.stderr  # CADR_BUILD_BOUNDS_CHECK
     cmd = [sys.executable, "-m", "pytest", "-q", "-x", "-m", "gpu", "-p", "no:cacheprovider",
            "-k", "not full_size", *[os.path.join(ROOT, "tests", m) for m in MODULES]]
     r = subprocess.run(cmd, env=env, cwd=ROOT, capture_output=True, text=True, timeout=1200)
