@@ -97,3 +97,16 @@ def test_null_arguments_are_rejected(cuda_lib):
     assert cuda_lib.cadr_server_submit(None, None, None, 0, None) == lib.INVALID_ARG
     assert cuda_lib.cadr_context_record_timestamp(None, 0, 0, None) == lib.INVALID_ARG
     assert cuda_lib.cadr_context_read_timestamps(None, 0, None) == lib.INVALID_ARG
+
+
+def test_bounds_checked_build_compiles_and_says_so(cuda_lib):
+    """The bounds-checked build (CADR_BOUNDS_CHECK) of the same sources
+    compiles for sm_103a, exports the same entry points and reports itself
+    through cadr_build_flags()."""
+    from cadr_gb300 import build
+    path = build.build_checked()
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    assert set(declared_symbols()) <= set(re.findall(r"\bT (cadr_\w+)", out))
+    checked = C.CDLL(path)
+    checked.cadr_build_flags.restype = C.c_uint32
+    assert checked.cadr_build_flags() == 1  # CADR_BUILD_BOUNDS_CHECK
