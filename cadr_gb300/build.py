@@ -40,19 +40,22 @@ def _stale(target: str, deps: list) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
+def _build_cuda(obj_dir: str, lib: str, defines: list, force: bool, ptxas_info: bool = False,
+                verbose: bool = False) -> str:
+    """Compiles every .cu under csrc into obj_dir (in parallel, skipping
+    objects newer than their sources and headers) and links them into lib."""
+    os.makedirs(obj_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "cadr_cuda.h"))
     srcs = sources()
-    objs = [os.path.join(OUT_DIR, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    objs = [os.path.join(obj_dir, os.path.basename(s)[:-3] + ".o") for s in srcs]
     extra = ["-Xptxas", "-v"] if ptxas_info else []
 
     def compile_one(pair):
         src, obj = pair
         if not force and not ptxas_info and not _stale(obj, [src] + headers):
             return ""
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *defines, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
@@ -64,11 +67,16 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
         for lg in logs:
             if lg:
                 sys.stderr.write(lg)
-    if force or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
+    if force or _stale(lib, objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return lib
+
+
+def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
+    _build_cuda(OUT_DIR, LIB, [], force, ptxas_info, verbose)
     build_facade(force=force)
     return LIB
 
@@ -82,29 +90,7 @@ def build_checked(force: bool = False) -> str:
     defined): every index a kernel derives itself is checked before the
     access it guards, a failed check sets CADR_DEVERR_BOUNDS and skips the
     access.  For tests on small cases; it is not the product library."""
-    os.makedirs(CHECKED_DIR, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(ROOT, "include", "cadr_cuda.h"))
-    srcs = sources()
-    objs = [os.path.join(CHECKED_DIR, os.path.basename(s)[:-3] + ".o") for s in srcs]
-
-    def compile_one(pair):
-        src, obj = pair
-        if not force and not _stale(obj, [src] + headers):
-            return
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-DCADR_BOUNDS_CHECK", "-c", src, "-o", obj]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
-
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        list(ex.map(compile_one, zip(srcs, objs)))
-    if force or _stale(CHECKED_LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", CHECKED_LIB, *objs, "-lcudart", "-lpthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    return CHECKED_LIB
+    return _build_cuda(CHECKED_DIR, CHECKED_LIB, ["-DCADR_BOUNDS_CHECK"], force)
 
 
 FACADE_DIR = os.path.join(HERE, "facade")
