@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
     if (t == 0) {
         sm.info[2] = load_relaxed_u32(a.tile_words + tile);
         cp_async_wait_all();
+#ifdef CADR_BOUNDS_CHECK
         // The scene's table against the offsets: the tile's first and last
         // drawables lie in its first and last regions.  (The command writes
         // check their own regions; this only reports a stale table.)
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(kLeafThreads, kWriteCtasPerSm) leaf_write_kern
         (void)CADR_CHECKED(rf <= rl && rl < a.num_state_sets && in_region(a.offsets, rf, b, b) &&
                                in_region(a.offsets, rl, e, e),
                            a.error);
+#endif
     }
     __syncthreads();
     LeafTile::scan_known_regions(sm);
