@@ -227,13 +227,27 @@ Renderer::Renderer(MemoryBackend& backend, bool makeDefault) : _backend(&backend
 Renderer::~Renderer()
 {
     if (_defaultRenderer == this) _defaultRenderer = nullptr;
+    finalize();
+    _storage.reset();
+    _ownBackend.reset();  // destroys the context this renderer created
+}
+
+void Renderer::finalize()
+{
     if (cadr_context* c = _backend->existingContext()) cadr_context_synchronize(c);
     if (_pack) cadr_pack_destroy(_pack);
     if (_drawables) _backend->freeBlock(_drawables);
     if (_indirect) _backend->freeBlock(_indirect);
     if (_pointers) _backend->freeBlock(_pointers);
-    _storage.reset();
-    _ownBackend.reset();  // destroys the context this renderer created
+    leakResources();
+}
+
+void Renderer::leakResources() noexcept
+{
+    _pack = nullptr;
+    _packCapacity = 0;
+    _drawables = _indirect = _pointers = 0;
+    _capacity = 0;
 }
 
 size_t Renderer::beginFrame()

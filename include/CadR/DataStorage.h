@@ -78,6 +78,7 @@ public:
     void upload(uint64_t dst, const void* src, size_t bytes) override;
     uint8_t* arena() const { return _arena; }
     size_t arenaBytes() const { return _bytes; }
+    size_t usedBlocks() const { return _used.size(); }
 
 private:
     uint8_t* _arena;

@@ -276,6 +276,20 @@ public:
 
     DataStorage& dataStorage() { return *_storage; }
     cadr_context* context() const { return _backend->context(); }
+    // Frees this renderer's own device buffers (the packed drawables, the
+    // indirect and pointer buffers, the device-resident pack) once the
+    // context's work has finished.  Idempotent; the destructor calls it
+    // (Renderer.cpp:89-94, 316-376).  As in the reference, the renderer
+    // is then only destroyed, not used; its DataStorage memory is freed with it.
+    void finalize();
+    // Forgets those buffers without freeing them, for a context whose
+    // device failed (Renderer.cpp:379-387).
+    void leakResources() noexcept;
+    // Alignment of the device blocks the renderer allocates (cudaMalloc
+    // gives 256 bytes), and an offset rounded up to it
+    // (Renderer.h:149-150, 228-229).
+    size_t standardBufferAlignment() const { return 256; }
+    size_t alignStandardBuffer(size_t offset) const { return (offset + 255) & ~size_t(255); }
     size_t frameNumber() const { return _frame; }
 
     size_t beginFrame();

@@ -498,6 +498,50 @@ static void check_cpu_times(const FrameInfo& f, const char* where)
            "%s: CPU timestamps out of order", where);
 }
 
+// Renderer::finalize / leakResources / standardBufferAlignment
+// (Renderer.cpp:89-94, 316-387; Renderer.h:228-229).
+static void test_finalize()
+{
+    HostMemoryBackend be(256 << 20);
+    Renderer r(be);
+    SceneBuild S;
+    r.beginFrame();
+    build_scene(r, S, 20, 500);
+    r.prepareSceneRendering(*S.root);
+    std::vector<DrawCall> calls;
+    r.recordSceneRendering(*S.root, calls);
+    r.executeCopyOperations();
+    const size_t used = be.usedBlocks();
+    EXPECT(r.drawableBufferAddress() && r.drawIndirectBufferAddress() && r.drawablePointersBufferAddress(),
+           "drawable buffers allocated");
+    r.finalize();
+    EXPECT(be.usedBlocks() == used - 3, "finalize freed %zu of the 3 drawable buffers", used - be.usedBlocks());
+    EXPECT(!r.drawableBufferAddress() && !r.drawIndirectBufferAddress() && !r.drawablePointersBufferAddress() &&
+               r.drawableBufferSize() == 0,
+           "buffers forgotten after finalize");
+    r.finalize();  // idempotent
+    EXPECT(be.usedBlocks() == used - 3, "a second finalize freed nothing more");
+    EXPECT(r.standardBufferAlignment() == 256 && r.alignStandardBuffer(0) == 0 && r.alignStandardBuffer(1) == 256 &&
+               r.alignStandardBuffer(256) == 256 && r.alignStandardBuffer(257) == 512,
+           "standard buffer alignment");
+    {
+        // leakResources: the buffers stay allocated, the renderer forgets them
+        HostMemoryBackend be2(64 << 20);
+        Renderer r2(be2, false);
+        SceneBuild S2;
+        r2.beginFrame();
+        build_scene(r2, S2, 5, 50);
+        r2.prepareSceneRendering(*S2.root);
+        std::vector<DrawCall> calls2;
+        r2.recordSceneRendering(*S2.root, calls2);
+        EXPECT(r2.drawableBufferAddress() != 0, "drawable buffers allocated");
+        const size_t used2 = be2.usedBlocks();
+        r2.leakResources();
+        EXPECT(!r2.drawableBufferAddress() && be2.usedBlocks() == used2, "leakResources frees nothing");
+    }
+    if (!g_fail) std::printf("finalize ok\n");
+}
+
 static void test_frame_info_host()
 {
     HostMemoryBackend be(64 << 20);
@@ -612,6 +656,7 @@ int main(int argc, char** argv)
             if (!g_fail) test_parent_child_lists();
             if (!g_fail) test_drawable_api();
             if (!g_fail) test_frame_info_host();
+            if (!g_fail) test_finalize();
         } else {
             test_gpu();
             if (!g_fail) test_gpu_resident();

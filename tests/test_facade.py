@@ -32,6 +32,7 @@ def test_facade_host_side(cuda_lib, oracle_lib, tmp_path):
     assert "parent/child lists ok" in r.stdout
     assert "drawable api ok" in r.stdout
     assert "frame info host ok" in r.stdout
+    assert "finalize ok" in r.stdout
     assert "facade cpu ok" in r.stdout
 
 
