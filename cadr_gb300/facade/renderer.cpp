@@ -215,12 +215,14 @@ Renderer::Renderer(int device, bool makeDefault)
     _ownBackend = std::make_unique<CudaMemoryBackend>(device);
     _backend = _ownBackend.get();
     _storage = std::make_unique<DataStorage>(*_backend);
+    _storage->setRenderer(this);
     if (makeDefault) _defaultRenderer = this;
 }
 
 Renderer::Renderer(MemoryBackend& backend, bool makeDefault) : _backend(&backend)
 {
     _storage = std::make_unique<DataStorage>(*_backend);
+    _storage->setRenderer(this);
     if (makeDefault) _defaultRenderer = this;
 }
 
@@ -254,6 +256,11 @@ size_t Renderer::beginFrame()
 {
     _frame++;
     _storage->setFrameNumber(_frame);
+    // the previous frame's uploads become the staging size hint
+    // (Renderer.cpp:394-397)
+    _lastFrameUploadBytes = _currentFrameUploadBytes;
+    _currentFrameUploadBytes = 0;
+    _storage->setStagingDataSizeHint(_lastFrameUploadBytes);
     _currentInfo = FrameInfo{};
     _currentInfo.frameNumber = _frame;
     _currentInfo.cpuBeginFrame = getCpuTimestamp();
@@ -348,7 +355,12 @@ void Renderer::recordSceneRendering(StateSet& root, std::vector<DrawCall>& out)
     _currentInfo.cpuRecordStateSetsEnd = getCpuTimestamp();
 }
 
-size_t Renderer::executeCopyOperations() { return _storage->uploadPending(); }
+size_t Renderer::executeCopyOperations()
+{
+    const size_t bytes = _storage->uploadPending();
+    _currentFrameUploadBytes += bytes;
+    return bytes;
+}
 
 void Renderer::recordDrawableProcessing(size_t n, cadr_stream stream)
 {

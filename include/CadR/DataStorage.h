@@ -28,6 +28,7 @@ namespace CadR {
 
 class DataMemory;
 class DataStorage;
+class Renderer;
 
 // Where device memory blocks come from and how bytes get there.
 class MemoryBackend {
@@ -181,7 +182,18 @@ public:
     DataAllocationRecord* realloc(DataAllocationRecord* a, size_t numBytes);
     void free(DataAllocationRecord* a) noexcept;
     DataAllocationRecord* zeroSizeAllocationRecord() { return &_zero; }
+    std::vector<DataMemory*>& dataMemoryList() { return _memories; }
     const std::vector<DataMemory*>& dataMemoryList() const { return _memories; }
+    // The renderer that owns this storage (DataStorage.h: renderer()); null
+    // for a storage made directly over a backend.
+    Renderer* renderer() const { return _renderer; }
+    void setRenderer(Renderer* r) noexcept { _renderer = r; }
+    // The bytes staged in the previous frame, which the reference uses to
+    // size its staging memory (Renderer.cpp:394-397); kept for callers that
+    // read it back.  Staged content here lives in per-allocation host
+    // buffers, so nothing else depends on it.
+    size_t stagingDataSizeHint() const { return _stagingHint; }
+    void setStagingDataSizeHint(size_t bytes) { _stagingHint = bytes; }
 
     // handles
     uint64_t createHandle() { return _handles.create(); }
@@ -208,6 +220,8 @@ private:
     DataAllocationRecord _zero;
     std::vector<DataAllocationRecord*> _pending;
     size_t _frame = ~size_t(0);
+    Renderer* _renderer = nullptr;
+    size_t _stagingHint = 0;
     HandleTable _handles;
     friend class DataMemory;
 };

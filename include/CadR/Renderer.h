@@ -346,6 +346,7 @@ private:
     uint32_t _gpuStamps = 0;             // timestamps the current frame recorded
     cadr_stream _frameStream = nullptr;  // the stream of the current frame's drawable processing
     size_t _endedFrame = ~size_t(0);     // the frame getFrameInfo() reports
+    size_t _lastFrameUploadBytes = 0, _currentFrameUploadBytes = 0;
     bool _endedHasGpu = false;
     uint64_t _endedGpuBase = 0;
     bool _layoutDirty = true;

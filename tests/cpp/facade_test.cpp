@@ -510,7 +510,13 @@ static void test_finalize()
     r.prepareSceneRendering(*S.root);
     std::vector<DrawCall> calls;
     r.recordSceneRendering(*S.root, calls);
-    r.executeCopyOperations();
+    const size_t uploaded = r.executeCopyOperations();
+    r.beginFrame();  // the previous frame's uploads become the staging hint (Renderer.cpp:394-397)
+    EXPECT(uploaded > 0 && r.dataStorage().stagingDataSizeHint() == uploaded, "staging size hint %zu of %zu",
+           r.dataStorage().stagingDataSizeHint(), uploaded);
+    r.beginFrame();
+    EXPECT(r.dataStorage().stagingDataSizeHint() == 0, "no uploads in the frame before");
+    EXPECT(r.dataStorage().renderer() == &r, "DataStorage::renderer()");
     const size_t used = be.usedBlocks();
     EXPECT(r.drawableBufferAddress() && r.drawIndirectBufferAddress() && r.drawablePointersBufferAddress(),
            "drawable buffers allocated");
