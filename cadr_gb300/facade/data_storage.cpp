@@ -330,6 +330,19 @@ DataAllocation::DataAllocation(DataAllocation&& o) noexcept : _storage(o._storag
     o._handle = 0;
 }
 
+DataAllocation& DataAllocation::operator=(DataAllocation&& o) noexcept
+{
+    if (this == &o) return *this;
+    free();
+    if (_handle) _storage->destroyHandle(_handle);
+    _storage = o._storage;
+    _record = o._record;
+    _handle = o._handle;
+    o._record = _storage->zeroSizeAllocationRecord();
+    o._handle = 0;
+    return *this;
+}
+
 DataAllocation::~DataAllocation()
 {
     free();

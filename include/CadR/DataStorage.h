@@ -244,7 +244,9 @@ class DataAllocation {
 public:
     explicit DataAllocation(DataStorage& storage);
     DataAllocation(DataAllocation&& other) noexcept;
-    DataAllocation& operator=(DataAllocation&&) = delete;
+    // Frees this allocation and its handle, then takes other's; other is
+    // left empty, without a handle (DataAllocation.h:64, 173).
+    DataAllocation& operator=(DataAllocation&& other) noexcept;
     DataAllocation(const DataAllocation&) = delete;
     ~DataAllocation();
 

@@ -85,6 +85,7 @@ public:
     Geometry(Geometry&&) = default;
     Geometry(const Geometry&) = delete;
     Geometry& operator=(const Geometry&) = delete;
+    Geometry& operator=(Geometry&&) = default;
     Renderer& renderer() const { return *_renderer; }
     DataStorage& dataStorage() const { return _vertices.dataStorage(); }
     size_t vertexDataSize() const { return _vertices.size(); }

@@ -72,8 +72,21 @@ int main()
     const Geometry& cg = g;
     EXPECT(std::memcmp(at(cg.indexDataAllocation().deviceAddress()), idx, sizeof(idx)) == 0,
            "index data staged and uploaded");
-    g.freeData();
-    EXPECT(g.vertexDataSize() == 0 && g.indexDataSize() == 0 && g.primitiveSetDataSize() == 0, "freeData");
+    // move assignment (DataAllocation.h:173, Geometry.h: operator=(Geometry&&))
+    Geometry g2(r);
+    const uint64_t vh = g.vertexDataAllocation().handle();
+    g2 = std::move(g);
+    EXPECT(g2.vertexDataSize() == sizeof(verts) && g2.vertexDataAllocation().handle() == vh &&
+               g.vertexDataSize() == 0 && g.vertexDataAllocation().handle() == 0,
+           "Geometry move assignment");
+    DataAllocation d1(r.dataStorage()), d2(r.dataStorage());
+    d2.upload(idx, sizeof(idx));
+    const uint64_t h2 = d2.handle();
+    d1 = std::move(d2);
+    EXPECT(d1.handle() == h2 && d1.size() == sizeof(idx) && d2.handle() == 0 && d2.size() == 0,
+           "DataAllocation move assignment");
+    g2.freeData();
+    EXPECT(g2.vertexDataSize() == 0 && g2.indexDataSize() == 0 && g2.primitiveSetDataSize() == 0, "freeData");
     if (!g_fail) std::printf("facade glm ok\n");
     return g_fail;
 }
