@@ -2,6 +2,7 @@
 // placement), DataStorage (64 KiB / 2 MiB / 32 MiB block strategy),
 // DataAllocation and HandlelessAllocation of the C++ facade.
 #include <CadR/DataStorage.h>
+#include <CadR/Renderer.h>
 
 #include <algorithm>
 #include <cstdlib>
@@ -319,16 +320,69 @@ size_t DataStorage::uploadPending()
 // ---------------------------------------------------------------------------
 // DataAllocation / HandlelessAllocation (DataAllocation.cpp:18-70).
 
+namespace {
+// The record of an allocation bound to no storage (DataAllocation(nullptr)).
+DataAllocationRecord g_nullRecord;
+DataAllocationRecord* emptyRecord(DataStorage* s) { return s ? s->zeroSizeAllocationRecord() : &g_nullRecord; }
+}  // namespace
+
+DataAllocation::DataAllocation(std::nullptr_t) noexcept : _storage(nullptr), _record(&g_nullRecord), _handle(0) {}
+
 DataAllocation::DataAllocation(DataStorage& storage)
     : _storage(&storage), _record(storage.zeroSizeAllocationRecord()), _handle(storage.createHandle())
 {
 }
 
+DataAllocation::DataAllocation(DataStorage& storage, noHandle_t) noexcept
+    : _storage(&storage), _record(storage.zeroSizeAllocationRecord()), _handle(0)
+{
+}
+
+DataAllocation::DataAllocation(Renderer& r) : DataAllocation(r.dataStorage()) {}
+
+DataAllocation::DataAllocation(Renderer& r, noHandle_t) noexcept : DataAllocation(r.dataStorage(), noHandle) {}
+
 DataAllocation::DataAllocation(DataAllocation&& o) noexcept : _storage(o._storage), _record(o._record), _handle(o._handle)
 {
-    o._record = _storage->zeroSizeAllocationRecord();
+    o._record = emptyRecord(_storage);
     o._handle = 0;
 }
+
+void DataAllocation::init(DataStorage& storage)
+{
+    free();
+    if (_handle && _storage != &storage) {
+        _storage->destroyHandle(_handle);
+        _handle = storage.createHandle();
+    }
+    _storage = &storage;
+    _record = storage.zeroSizeAllocationRecord();
+}
+
+StagingData DataAllocation::alloc()
+{
+    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record);
+    return alloc(_record->size);
+}
+
+uint64_t DataAllocation::createHandle(DataStorage& storage)
+{
+    if (_handle == 0) {
+        _storage = &storage;
+        _handle = storage.createHandle();
+        if (_record->size) storage.setHandle(_handle, _record->deviceAddress);
+    }
+    return _handle;
+}
+
+void DataAllocation::destroyHandle() noexcept
+{
+    if (_handle == 0) return;
+    _storage->destroyHandle(_handle);
+    _handle = 0;
+}
+
+size_t DataAllocation::offset() const { return size_t(_record->deviceAddress - _record->dataMemory->deviceAddress()); }
 
 DataAllocation& DataAllocation::operator=(DataAllocation&& o) noexcept
 {
@@ -338,13 +392,14 @@ DataAllocation& DataAllocation::operator=(DataAllocation&& o) noexcept
     _storage = o._storage;
     _record = o._record;
     _handle = o._handle;
-    o._record = _storage->zeroSizeAllocationRecord();
+    o._record = emptyRecord(_storage);
     o._handle = 0;
     return *this;
 }
 
 DataAllocation::~DataAllocation()
 {
+    if (!_storage) return;
     free();
     if (_handle) _storage->destroyHandle(_handle);
 }

@@ -242,7 +242,14 @@ private:
 // An allocation with a handle (DataAllocation.h:45-96).
 class DataAllocation {
 public:
+    enum class noHandle_t : int;
+    static constexpr noHandle_t noHandle = noHandle_t(0);
+    // An allocation of no storage and no handle, to be init()-ed later.
+    explicit DataAllocation(std::nullptr_t) noexcept;
     explicit DataAllocation(DataStorage& storage);
+    DataAllocation(DataStorage& storage, noHandle_t) noexcept;  // without a handle
+    explicit DataAllocation(Renderer& r);
+    DataAllocation(Renderer& r, noHandle_t) noexcept;
     DataAllocation(DataAllocation&& other) noexcept;
     // Frees this allocation and its handle, then takes other's; other is
     // left empty, without a handle (DataAllocation.h:64, 173).
@@ -250,14 +257,36 @@ public:
     DataAllocation(const DataAllocation&) = delete;
     ~DataAllocation();
 
+    // Frees the memory (the handle stays) and binds to `storage`.
+    void init(DataStorage& storage);
+    // New content of numBytes; reuses this frame's staging when it fits
+    // (DataAllocation.cpp:18-34).
     StagingData alloc(size_t numBytes);
+    // New content of the current size; this frame's staging if there is
+    // one already (DataAllocation.cpp:37-51).
+    StagingData alloc();
+    StagingData createStagingData() { return alloc(); }
+    StagingData createStagingData(size_t numBytes) { return alloc(numBytes); }
     void free() noexcept;
+    // A handle for an allocation made without one, pointed at its current
+    // memory (the reference's leaves the entry unset until the next
+    // alloc); returns the handle.
+    uint64_t createHandle(DataStorage& storage);
+    void destroyHandle() noexcept;
     void upload(const void* ptr, size_t numBytes);
     void setData(const void* ptr, size_t numBytes) { upload(ptr, numBytes); }
+    template <typename T> void setData(const T& data) { upload(&data, sizeof(data)); }
+    template <typename T> T& editNewContent() { return *alloc(sizeof(T)).template data<T>(); }
+    template <typename T> T* editNewContent(size_t count) { return alloc(sizeof(T) * count).template data<T>(); }
     uint64_t handle() const { return _handle; }
     uint64_t deviceAddress() const { return _record->deviceAddress; }
     size_t size() const { return _record->size; }
+    // The DataMemory block holding a non-empty allocation, and the
+    // allocation's offset inside it.
+    DataMemory& dataMemory() const { return *_record->dataMemory; }
+    size_t offset() const;
     DataStorage& dataStorage() const { return *_storage; }
+    Renderer& renderer() const { return *_storage->renderer(); }
 
 private:
     DataStorage* _storage;

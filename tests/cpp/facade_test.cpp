@@ -548,6 +548,53 @@ static void test_finalize()
     if (!g_fail) std::printf("finalize ok\n");
 }
 
+// DataAllocation's construction forms, staging and handle functions
+// (DataAllocation.h:54-96, 150-212; DataAllocation.cpp:18-51).
+static void test_data_allocation_api()
+{
+    HostMemoryBackend be(16 << 20);
+    Renderer r(be, false);
+    DataStorage& ds = r.dataStorage();
+    r.beginFrame();
+    DataAllocation a(nullptr);
+    EXPECT(a.handle() == 0 && a.size() == 0, "an allocation of no storage");
+    a.init(ds);
+    EXPECT(a.handle() == 0 && &a.dataStorage() == &ds, "init binds the storage, no handle");
+    struct Rec {
+        uint32_t x, y;
+    };
+    a.setData(Rec{7, 9});
+    Rec& e = a.editNewContent<Rec>();  // the same frame and size: the same staging
+    e.y = 11;
+    const uint64_t h = a.createHandle(ds);
+    EXPECT(h != 0 && a.createHandle(ds) == h, "createHandle makes one handle");
+    DataAllocation b(r, DataAllocation::noHandle);
+    uint32_t* words = b.editNewContent<uint32_t>(4);
+    for (uint32_t k = 0; k < 4; k++) words[k] = 100 + k;
+    DataAllocation c(r);
+    EXPECT(b.handle() == 0 && c.handle() != 0 && c.handle() != h, "handles");
+    r.executeCopyOperations();
+    const Rec* dev = reinterpret_cast<const Rec*>(a.deviceAddress());
+    EXPECT(dev->x == 7 && dev->y == 11, "setData then editNewContent: %u %u", dev->x, dev->y);
+    EXPECT(ds.handleLevel() == 1 &&
+               reinterpret_cast<const uint64_t*>(ds.handleTableDeviceAddress())[h] == a.deviceAddress(),
+           "the handle made after the data resolves to it");
+    EXPECT(a.offset() == a.deviceAddress() - a.dataMemory().deviceAddress() && a.offset() < a.dataMemory().size(),
+           "offset inside its DataMemory");
+    EXPECT(&a.renderer() == &r, "renderer()");
+    r.beginFrame();
+    StagingData sd = b.alloc();  // a new frame: new content of the current size
+    EXPECT(sd.size() == 16, "alloc() keeps the size");
+    std::memset(sd.data(), 0xab, 16);
+    EXPECT(b.createStagingData().data() == sd.data(), "the frame's staging is reused");
+    r.executeCopyOperations();
+    const uint8_t* bytes = reinterpret_cast<const uint8_t*>(b.deviceAddress());
+    EXPECT(bytes[0] == 0xab && bytes[15] == 0xab, "alloc() content uploaded");
+    a.destroyHandle();
+    EXPECT(a.handle() == 0, "destroyHandle");
+    if (!g_fail) std::printf("data allocation api ok\n");
+}
+
 static void test_frame_info_host()
 {
     HostMemoryBackend be(64 << 20);
@@ -663,6 +710,7 @@ int main(int argc, char** argv)
             if (!g_fail) test_drawable_api();
             if (!g_fail) test_frame_info_host();
             if (!g_fail) test_finalize();
+            if (!g_fail) test_data_allocation_api();
         } else {
             test_gpu();
             if (!g_fail) test_gpu_resident();

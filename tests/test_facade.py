@@ -33,6 +33,7 @@ def test_facade_host_side(cuda_lib, oracle_lib, tmp_path):
     assert "drawable api ok" in r.stdout
     assert "frame info host ok" in r.stdout
     assert "finalize ok" in r.stdout
+    assert "data allocation api ok" in r.stdout
     assert "facade cpu ok" in r.stdout
 
 
