@@ -430,17 +430,47 @@ void DataAllocation::upload(const void* p, size_t n)
     if (n) std::memcpy(s.data(), p, n);
 }
 
+HandlelessAllocation::HandlelessAllocation(std::nullptr_t) noexcept : _storage(nullptr), _record(&g_nullRecord) {}
+
 HandlelessAllocation::HandlelessAllocation(DataStorage& storage)
     : _storage(&storage), _record(storage.zeroSizeAllocationRecord())
 {
 }
 
+HandlelessAllocation::HandlelessAllocation(Renderer& r) : HandlelessAllocation(r.dataStorage()) {}
+
 HandlelessAllocation::HandlelessAllocation(HandlelessAllocation&& o) noexcept : _storage(o._storage), _record(o._record)
 {
-    o._record = _storage->zeroSizeAllocationRecord();
+    o._record = emptyRecord(_storage);
 }
 
-HandlelessAllocation::~HandlelessAllocation() { free(); }
+HandlelessAllocation& HandlelessAllocation::operator=(HandlelessAllocation&& o) noexcept
+{
+    if (this == &o) return *this;
+    free();
+    _storage = o._storage;
+    _record = o._record;
+    o._record = emptyRecord(_storage);
+    return *this;
+}
+
+HandlelessAllocation::~HandlelessAllocation()
+{
+    if (_storage) free();
+}
+
+void HandlelessAllocation::init(DataStorage& storage)
+{
+    free();
+    _storage = &storage;
+    _record = storage.zeroSizeAllocationRecord();
+}
+
+StagingData HandlelessAllocation::alloc()
+{
+    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record);
+    return alloc(_record->size);
+}
 
 StagingData HandlelessAllocation::alloc(size_t n)
 {

@@ -297,16 +297,34 @@ private:
 // An allocation without a handle.
 class HandlelessAllocation {
 public:
+    explicit HandlelessAllocation(std::nullptr_t) noexcept;
     explicit HandlelessAllocation(DataStorage& storage);
+    explicit HandlelessAllocation(Renderer& r);
     HandlelessAllocation(HandlelessAllocation&& other) noexcept;
-    HandlelessAllocation& operator=(HandlelessAllocation&&) = delete;
+    HandlelessAllocation& operator=(HandlelessAllocation&& other) noexcept;
     HandlelessAllocation(const HandlelessAllocation&) = delete;
     ~HandlelessAllocation();
 
+    void init(DataStorage& storage);
     StagingData alloc(size_t numBytes);
+    StagingData alloc();
+    StagingData createStagingData() { return alloc(); }
+    StagingData createStagingData(size_t numBytes) { return alloc(numBytes); }
     void free() noexcept;
+    void setData(const void* ptr, size_t numBytes)
+    {
+        StagingData s = alloc(numBytes);
+        if (numBytes) std::memcpy(s.data(), ptr, numBytes);
+    }
+    template <typename T> void setData(const T& data) { setData(&data, sizeof(data)); }
+    template <typename T> T& editNewContent() { return *alloc(sizeof(T)).template data<T>(); }
+    template <typename T> T* editNewContent(size_t count) { return alloc(sizeof(T) * count).template data<T>(); }
     uint64_t deviceAddress() const { return _record->deviceAddress; }
     size_t size() const { return _record->size; }
+    DataMemory& dataMemory() const { return *_record->dataMemory; }
+    size_t offset() const { return size_t(_record->deviceAddress - _record->dataMemory->deviceAddress()); }
+    DataStorage& dataStorage() const { return *_storage; }
+    Renderer& renderer() const { return *_storage->renderer(); }
 
 private:
     DataStorage* _storage;

@@ -592,6 +592,15 @@ static void test_data_allocation_api()
     EXPECT(bytes[0] == 0xab && bytes[15] == 0xab, "alloc() content uploaded");
     a.destroyHandle();
     EXPECT(a.handle() == 0, "destroyHandle");
+    // HandlelessAllocation: the same forms without a handle
+    HandlelessAllocation u(nullptr), v(r);
+    u.init(ds);
+    u.setData(Rec{1, 2});
+    v = std::move(u);
+    EXPECT(v.size() == sizeof(Rec) && u.size() == 0 && &v.renderer() == &r, "handleless move assignment");
+    r.executeCopyOperations();
+    EXPECT(reinterpret_cast<const Rec*>(v.deviceAddress())->y == 2 && v.offset() < v.dataMemory().size(),
+           "handleless content and offset");
     if (!g_fail) std::printf("data allocation api ok\n");
 }
 
