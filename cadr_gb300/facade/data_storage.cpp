@@ -361,7 +361,7 @@ void DataAllocation::init(DataStorage& storage)
 
 StagingData DataAllocation::alloc()
 {
-    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record);
+    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record, false);
     return alloc(_record->size);
 }
 
@@ -406,7 +406,8 @@ DataAllocation::~DataAllocation()
 
 StagingData DataAllocation::alloc(size_t n)
 {
-    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber() && n <= _record->size) {
+    const bool reuse = _record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber() && n <= _record->size;
+    if (reuse) {
         _record->size = n;
     } else {
         _record = _storage->realloc(_record, n);
@@ -414,7 +415,7 @@ StagingData DataAllocation::alloc(size_t n)
     }
     _record->staging.resize(_record->size);
     _storage->markPending(_record);
-    return StagingData(_record);
+    return StagingData(_record, !reuse);
 }
 
 void DataAllocation::free() noexcept
@@ -468,19 +469,20 @@ void HandlelessAllocation::init(DataStorage& storage)
 
 StagingData HandlelessAllocation::alloc()
 {
-    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record);
+    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber()) return StagingData(_record, false);
     return alloc(_record->size);
 }
 
 StagingData HandlelessAllocation::alloc(size_t n)
 {
-    if (_record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber() && n <= _record->size)
+    const bool reuse = _record->size != 0 && _record->stagingFrameNumber == _storage->frameNumber() && n <= _record->size;
+    if (reuse)
         _record->size = n;
     else
         _record = _storage->realloc(_record, n);
     _record->staging.resize(_record->size);
     _storage->markPending(_record);
-    return StagingData(_record);
+    return StagingData(_record, !reuse);
 }
 
 void HandlelessAllocation::free() noexcept

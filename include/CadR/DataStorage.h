@@ -230,13 +230,19 @@ private:
 // Renderer::executeCopyOperations (StagingData.h in the reference).
 class StagingData {
 public:
-    explicit StagingData(DataAllocationRecord* r) : _r(r) {}
+    StagingData() = default;
+    // wasReallocated: the allocation moved to new memory for this content,
+    // so all of it is to be written (StagingData.h: wasReallocated()).
+    explicit StagingData(DataAllocationRecord* r, bool wasReallocated = true) : _r(r), _realloc(wasReallocated) {}
     void* data() const { return _r->staging.data(); }
     template <typename T> T* data() const { return reinterpret_cast<T*>(_r->staging.data()); }
     size_t size() const { return _r->size; }
+    size_t sizeInBytes() const { return _r->size; }
+    bool wasReallocated() const { return _realloc; }
 
 private:
-    DataAllocationRecord* _r;
+    DataAllocationRecord* _r = nullptr;
+    bool _realloc = false;
 };
 
 // An allocation with a handle (DataAllocation.h:45-96).

@@ -586,7 +586,11 @@ static void test_data_allocation_api()
     StagingData sd = b.alloc();  // a new frame: new content of the current size
     EXPECT(sd.size() == 16, "alloc() keeps the size");
     std::memset(sd.data(), 0xab, 16);
-    EXPECT(b.createStagingData().data() == sd.data(), "the frame's staging is reused");
+    EXPECT(sd.wasReallocated() && sd.sizeInBytes() == 16, "a new frame's content is new memory");
+    StagingData again = b.createStagingData();
+    EXPECT(again.data() == sd.data() && !again.wasReallocated(), "the frame's staging is reused");
+    StagingData none;
+    (void)none;
     r.executeCopyOperations();
     const uint8_t* bytes = reinterpret_cast<const uint8_t*>(b.deviceAddress());
     EXPECT(bytes[0] == 0xab && bytes[15] == 0xab, "alloc() content uploaded");
