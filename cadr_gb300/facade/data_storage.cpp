@@ -203,8 +203,8 @@ DataStorage::DataStorage(MemoryBackend& backend) : _backend(&backend), _handles(
 
 DataStorage::~DataStorage()
 {
-    _handles.~HandleTable();
-    new (&_handles) HandleTable(*this);
+    // The tables live in this storage's memory: free them before it goes.
+    _handles.destroyAll();
     _pending.clear();
     for (DataMemory* m : _memories) {
         _backend->freeBlock(m->deviceAddress());

@@ -15,10 +15,20 @@
 
 namespace CadR {
 
-HandleTable::~HandleTable()
+HandleTable::~HandleTable() { destroyAll(); }
+
+// Frees every table's memory and forgets every handle (the reference's
+// HandleTable::destroyAll, called by DataStorage::cleanUp()).
+void HandleTable::destroyAll() noexcept
 {
     for (auto& t : _tables)
         if (t->record) _storage->free(t->record);
+    _tables.clear();
+    _root = nullptr;
+    _llt.clear();
+    _l1.clear();
+    _level = 0;
+    _highest = 0;
 }
 
 HandleTable::Table* HandleTable::newTable()

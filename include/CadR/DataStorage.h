@@ -144,6 +144,7 @@ public:
     uint64_t create();
     void set(uint64_t handle, uint64_t addr);
     void destroy(uint64_t handle) noexcept { (void)handle; }  // handles are not recycled, as in the reference
+    void destroyAll() noexcept;
     unsigned handleLevel() const { return _level; }
     uint64_t rootTableDeviceAddress() const;
     uint64_t highestHandle() const { return _highest; }
