@@ -17,8 +17,8 @@ namespace CadR {
 
 HandleTable::~HandleTable() { destroyAll(); }
 
-// Frees every table's memory and forgets every handle (HandleTable.h:
-// destroyAll()); the storage calls it before its memory is released.
+// Frees every table's memory and forgets every handle (HandleTable.h:102,
+// HandleTable.cpp:85); the storage calls it before its memory is released.
 void HandleTable::destroyAll() noexcept
 {
     for (auto& t : _tables)
