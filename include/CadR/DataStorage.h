@@ -252,10 +252,11 @@ public:
     enum class noHandle_t : int;
     static constexpr noHandle_t noHandle = noHandle_t(0);
     // An allocation of no storage and no handle, to be init()-ed later.
-    explicit DataAllocation(std::nullptr_t) noexcept;
-    explicit DataAllocation(DataStorage& storage);
+    // The constructors are implicit, as the reference's are.
+    DataAllocation(std::nullptr_t) noexcept;
+    DataAllocation(DataStorage& storage);
     DataAllocation(DataStorage& storage, noHandle_t) noexcept;  // without a handle
-    explicit DataAllocation(Renderer& r);
+    DataAllocation(Renderer& r);
     DataAllocation(Renderer& r, noHandle_t) noexcept;
     DataAllocation(DataAllocation&& other) noexcept;
     // Frees this allocation and its handle, then takes other's; other is
@@ -304,9 +305,9 @@ private:
 // An allocation without a handle.
 class HandlelessAllocation {
 public:
-    explicit HandlelessAllocation(std::nullptr_t) noexcept;
-    explicit HandlelessAllocation(DataStorage& storage);
-    explicit HandlelessAllocation(Renderer& r);
+    HandlelessAllocation(std::nullptr_t) noexcept;
+    HandlelessAllocation(DataStorage& storage);
+    HandlelessAllocation(Renderer& r);
     HandlelessAllocation(HandlelessAllocation&& other) noexcept;
     HandlelessAllocation& operator=(HandlelessAllocation&& other) noexcept;
     HandlelessAllocation(const HandlelessAllocation&) = delete;

@@ -556,7 +556,7 @@ static void test_data_allocation_api()
     Renderer r(be, false);
     DataStorage& ds = r.dataStorage();
     r.beginFrame();
-    DataAllocation a(nullptr);
+    DataAllocation a = nullptr;  // implicit, as in CadR
     EXPECT(a.handle() == 0 && a.size() == 0, "an allocation of no storage");
     a.init(ds);
     EXPECT(a.handle() == 0 && &a.dataStorage() == &ds, "init binds the storage, no handle");
