@@ -81,7 +81,7 @@ class StateSet;
 
 class Geometry {
 public:
-    explicit Geometry(Renderer& r);
+    Geometry(Renderer& r);
     Geometry(Geometry&&) = default;
     Geometry(const Geometry&) = delete;
     Geometry& operator=(const Geometry&) = delete;
@@ -120,7 +120,7 @@ private:
 
 class MatrixList {
 public:
-    explicit MatrixList(Renderer& r);
+    MatrixList(Renderer& r);
     MatrixList(MatrixList&&) = default;
     void setMatrices(const Mat4& m) { setMatrixData(&m, 1); }
     void setMatrices(const std::vector<Mat4>& m) { setMatrixData(m.data(), m.size()); }
@@ -182,7 +182,7 @@ struct DrawCall {
 
 class StateSet {
 public:
-    explicit StateSet(Renderer& r) : _renderer(&r) {}
+    StateSet(Renderer& r) : _renderer(&r) {}
     ~StateSet();
     StateSet(const StateSet&) = delete;
     StateSet& operator=(const StateSet&) = delete;
