@@ -387,8 +387,8 @@ CADR_API cadr_status cadr_context_read_timestamps(cadr_context* ctx, uint64_t fr
 
 CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault)
 {
-    if (!ctx || fault > CADR_FAULT_SKIP_FIRST_TILE_PUBLISH) return fail(CADR_ERR_INVALID_ARG, "debug_set_fault: bad argument");
-    ctx->fault = fault;
+    if (!ctx || fault > CADR_FAULT_SERVER_LAUNCH) return fail(CADR_ERR_INVALID_ARG, "debug_set_fault: bad argument");
+    __atomic_store_n(&ctx->fault, fault, __ATOMIC_RELAXED);  // the server's scheduler thread reads it
     return CADR_OK;
 }
 

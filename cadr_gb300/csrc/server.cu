@@ -167,6 +167,8 @@ static void CUDART_CB on_slot_done(void* p)
 static cadr_status launch_slot(cadr_server* srv, Slot* slot, std::vector<Request*>& batch)
 {
     cadr_context* ctx = srv->ctx;
+    if (__atomic_load_n(&ctx->fault, __ATOMIC_RELAXED) == CADR_FAULT_SERVER_LAUNCH)
+        return fail(CADR_ERR_CUDA, "server: launch failed (injected by CADR_FAULT_SERVER_LAUNCH)");
     const cadr_tuning tu = ctx->tuning;
     uint32_t nv = 0;
     for (Request* r : batch) nv += r->num_views;
@@ -282,9 +284,13 @@ static void worker_main(cadr_server* srv)
         srv->inflight++;
         lk.unlock();
         cadr_status st = launch_slot(srv, slot, batch);
+        // Whatever of a failed batch reached the stream has finished before
+        // its output memory goes back to the arena.
+        if (st != CADR_OK) cudaStreamSynchronize(slot->stream);
         lk.lock();
         if (st != CADR_OK) {
             for (Request* r : batch) {
+                srv->arena.free(r->out_off, r->out_bytes);  // a failed request keeps no output
                 r->status = st;
                 r->done = true;
                 r->complete_ns = now_ns();

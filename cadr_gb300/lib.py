@@ -23,7 +23,7 @@ STATUS = {0: "CADR_OK", 1: "CADR_ERR_INVALID_ARG", 2: "CADR_ERR_OUT_OF_MEMORY", 
           4: "CADR_ERR_CUDA", 5: "CADR_ERR_DEVICE", 6: "CADR_ERR_NOT_READY", 7: "CADR_ERR_REJECTED"}
 OK, INVALID_ARG, OUT_OF_MEMORY, TIMEOUT, CUDA, DEVICE, NOT_READY, REJECTED = range(8)
 DEVERR_LOOKBACK_TIMEOUT, DEVERR_MBARRIER_TIMEOUT, DEVERR_BAD_INDEX, DEVERR_BOUNDS = 0x1, 0x2, 0x4, 0x8
-FAULT_NONE, FAULT_SKIP_FIRST_TILE_PUBLISH = 0, 1
+FAULT_NONE, FAULT_SKIP_FIRST_TILE_PUBLISH, FAULT_SERVER_LAUNCH = 0, 1, 2
 
 # Exported symbols of the C ABI (checked against include/cadr_cuda.h by the tests).
 vp, u32, u64, i32, sz = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_size_t
@@ -620,7 +620,8 @@ class Server:
     def poll(self):
         n = u32()
         check(self.ctx.lib.cadr_server_poll(self.handle, self._res, 256, C.byref(n)))
-        return [self._res[i] for i in range(n.value)]
+        # copies: the next poll reuses the buffer
+        return [RequestResult.from_buffer_copy(self._res[i]) for i in range(n.value)]
 
     def release(self, rid: int):
         check(self.ctx.lib.cadr_server_release(self.handle, rid))

@@ -554,6 +554,11 @@ CADR_API cadr_status cadr_context_check_device_error(cadr_context* ctx, uint32_t
  * ends; the context stays usable.  (The plain pass has no waits.) */
 #define CADR_FAULT_NONE 0u
 #define CADR_FAULT_SKIP_FIRST_TILE_PUBLISH 1u
+/* Host side, for the serving tests: while set, every batch a server on this
+ * context admits fails before anything is launched, as a failed launch
+ * would; its requests finish with CADR_ERR_CUDA and give their output
+ * memory back.  No GPU work is involved. */
+#define CADR_FAULT_SERVER_LAUNCH 2u
 CADR_API cadr_status cadr_debug_set_fault(cadr_context* ctx, uint32_t fault);
 
 /* ------------------------------------------------------------------------ */

@@ -85,3 +85,41 @@ def test_admission_by_memory(ctx, resident):
         time.sleep(0.001)
     assert sorted(got) == sorted(ids)
     srv.close()
+
+
+def test_failed_batches_give_their_memory_back(ctx, resident):
+    """A batch whose launch fails (CADR_FAULT_SERVER_LAUNCH: on the host,
+    before anything is launched) ends its requests with CADR_ERR_CUDA and
+    returns their output memory: six requests that fit three at a time all
+    fail in turn, and afterwards three requests that need the whole budget
+    are admitted together and complete."""
+    scs, dss = resident
+    per_view = ((scs[2].n * 20 + 255) // 256) * 256 + 1024
+    srv = lib.Server(ctx, max_inflight=2, max_batch_views=4, window_ns=50_000, memory_budget=3 * per_view)
+    ctx.set_fault(lib.FAULT_SERVER_LAUNCH)
+    try:
+        failed = [srv.submit(dss[2], scenes.random_view(4, 700 + j)) for j in range(6)]
+        got = {}
+        deadline = time.time() + 30
+        while len(got) < len(failed) and time.time() < deadline:
+            for r in srv.poll():
+                got[r.request_id] = r
+            time.sleep(0.001)
+    finally:
+        ctx.set_fault(lib.FAULT_NONE)
+    assert sorted(got) == sorted(failed)
+    assert all(r.status == lib.CUDA for r in got.values())
+    for rid in failed:
+        srv.release(rid)
+    ids = [srv.submit(dss[2], scenes.random_view(4, 800 + j)) for j in range(3)]
+    done = {}
+    deadline = time.time() + 30
+    while len(done) < len(ids) and time.time() < deadline:
+        for r in srv.poll():
+            done[r.request_id] = r
+        time.sleep(0.001)
+    assert sorted(done) == sorted(ids)
+    assert all(r.status == lib.OK for r in done.values())
+    for rid in ids:
+        srv.release(rid)
+    srv.close()
