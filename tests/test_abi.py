@@ -110,3 +110,19 @@ def test_bounds_checked_build_compiles_and_says_so(cuda_lib):
     checked = C.CDLL(path)
     checked.cadr_build_flags.restype = C.c_uint32
     assert checked.cadr_build_flags() == 1  # CADR_BUILD_BOUNDS_CHECK
+
+
+def test_headers_compile_on_their_own(tmp_path):
+    """Each public header compiles by itself: cadr_cuda.h as C99 and C++17,
+    every include/CadR header as C++17 (a drop-in user includes them one by
+    one, as CadR's own headers are included)."""
+    inc = os.path.join(ROOT, "include")
+    c = tmp_path / "h.c"
+    c.write_text("#include <cadr_cuda.h>\n")
+    subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-I", inc, str(c)], check=True)
+    for h in ["cadr_cuda.h"] + ["CadR/" + f for f in sorted(os.listdir(os.path.join(inc, "CadR"))) if f.endswith(".h")]:
+        src = tmp_path / "h.cpp"
+        src.write_text(f"#include <{h}>\n")
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-I", inc, str(src)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, h + "\n" + r.stderr[-2000:]
